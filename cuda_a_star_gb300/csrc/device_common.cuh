@@ -1,0 +1,507 @@
+// Device building blocks of the GA* engine: entries, warp sorting networks,
+// the warp-cooperative batched binary heap and the duplicate-detection tables.
+//
+// Reference (michalborkowski96/cuda_a_star) counterparts:
+//   HeapEntry / QueueValue ordering        heaps.h:14-23, a_star.h:55-66
+//   HeapsDevice::extract/insert/remove     heaps.h:93-160   -> WarpHeap (below)
+//   FancyHashmap mass insert + statuses    fancy_hashmap.h:32-167, 336-340
+//                                          -> insert-or-min with CAS (below)
+//   bitonic_sort network (global memory)   bitonic_sort.h:107-143
+//                                          -> register/shuffle networks (below)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gastar {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint64_t kEmpty = ~0ull;      // empty table key / value
+constexpr uint64_t kInfPrio = ~0ull;    // priority of a padding entry
+constexpr uint32_t kInf = 0xffffffffu;
+constexpr uint32_t kRootMove = 0xffu;   // parent move of the start state
+
+// Device status codes; the numeric values are the gastar_status values of the C ABI.
+enum : uint32_t {
+    ST_OK = 0, ST_NO_PATH = 1, ST_BUDGET = 2, ST_TIMEOUT = 3, ST_HEAP_FULL = 4,
+    ST_TABLE_FULL = 5, ST_PATH_CAP = 6, ST_BARRIER = 7, ST_BAD_INPUT = 8,
+};
+enum : uint32_t { LIFE_FRESH = 0, LIFE_RUNNING = 1, LIFE_DONE = 2 };
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    // SplitMix64 output function (Steele, Lea, Flood 2014).
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+// Priority word: f in the high half, (2^32-1 - g) in the low half, so that
+// one unsigned comparison gives the reference's order "lower f first, equal
+// f -> higher g first" (QueueValue::operator<, a_star.h:58-63).
+__host__ __device__ __forceinline__ uint64_t make_prio(uint32_t f, uint32_t g) {
+    return (uint64_t(f) << 32) | uint64_t(0xffffffffu - g);
+}
+__host__ __device__ __forceinline__ uint32_t prio_f(uint64_t p) { return uint32_t(p >> 32); }
+__host__ __device__ __forceinline__ uint32_t prio_g(uint64_t p) { return 0xffffffffu - uint32_t(p); }
+
+// Table value word: g in the high half, parent move in the low byte; one
+// 64-bit atomicMin keeps the lowest g and, among equal g, the lowest move.
+__host__ __device__ __forceinline__ uint64_t make_val(uint32_t g, uint32_t move) {
+    return (uint64_t(g) << 32) | move;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// Heap entries: 16 bytes for 64-bit state keys, 32 bytes for 128-bit keys.
+// ---------------------------------------------------------------------------
+template <int KW> struct Entry;
+template <> struct alignas(16) Entry<1> { uint64_t prio, k0; };
+template <> struct alignas(16) Entry<2> { uint64_t prio, k0, k1, pad; };
+
+template <int KW> __device__ __forceinline__ Entry<KW> inf_entry() {
+    Entry<KW> e;
+    e.prio = kInfPrio;
+    e.k0 = 0;
+    if constexpr (KW == 2) { e.k1 = 0; e.pad = 0; }
+    return e;
+}
+
+template <int KW> __device__ __forceinline__ Entry<KW> shfl_idx(const Entry<KW>& e, int src) {
+    Entry<KW> r;
+    r.prio = __shfl_sync(kFull, e.prio, src);
+    r.k0 = __shfl_sync(kFull, e.k0, src);
+    if constexpr (KW == 2) { r.k1 = __shfl_sync(kFull, e.k1, src); r.pad = 0; }
+    return r;
+}
+
+template <int KW> __device__ __forceinline__ Entry<KW> shfl_xor(const Entry<KW>& e, int m) {
+    Entry<KW> r;
+    r.prio = __shfl_xor_sync(kFull, e.prio, m);
+    r.k0 = __shfl_xor_sync(kFull, e.k0, m);
+    if constexpr (KW == 2) { r.k1 = __shfl_xor_sync(kFull, e.k1, m); r.pad = 0; }
+    return r;
+}
+
+// L2-coherent loads/stores (heap nodes and stage buffers are handed between
+// launches and, in multi-block teams, between blocks).
+template <int KW> __device__ __forceinline__ Entry<KW> ld_entry(const Entry<KW>* p) {
+    Entry<KW> e;
+    uint4 a = __ldcg(reinterpret_cast<const uint4*>(p));
+    e.prio = (uint64_t(a.y) << 32) | a.x;
+    e.k0 = (uint64_t(a.w) << 32) | a.z;
+    if constexpr (KW == 2) {
+        uint4 b = __ldcg(reinterpret_cast<const uint4*>(p) + 1);
+        e.k1 = (uint64_t(b.y) << 32) | b.x;
+        e.pad = 0;
+    }
+    return e;
+}
+template <int KW> __device__ __forceinline__ void st_entry(Entry<KW>* p, const Entry<KW>& e) {
+    uint4 a = make_uint4(uint32_t(e.prio), uint32_t(e.prio >> 32), uint32_t(e.k0), uint32_t(e.k0 >> 32));
+    __stcg(reinterpret_cast<uint4*>(p), a);
+    if constexpr (KW == 2) {
+        uint4 b = make_uint4(uint32_t(e.k1), uint32_t(e.k1 >> 32), 0u, 0u);
+        __stcg(reinterpret_cast<uint4*>(p) + 1, b);
+    }
+}
+
+// Stage-buffer access: shared memory for one-block teams (plain generic
+// accesses), global memory shared by the blocks of a multi-block team
+// (L2-coherent accesses, since the buffer is refilled every iteration).
+template <int KW> __device__ __forceinline__ Entry<KW> ld_stage(const Entry<KW>* p, bool global) {
+    if (global) return ld_entry(p);
+    Entry<KW> e;
+    const uint4 a = *reinterpret_cast<const uint4*>(p);
+    e.prio = (uint64_t(a.y) << 32) | a.x;
+    e.k0 = (uint64_t(a.w) << 32) | a.z;
+    if constexpr (KW == 2) {
+        const uint4 b = *(reinterpret_cast<const uint4*>(p) + 1);
+        e.k1 = (uint64_t(b.y) << 32) | b.x;
+        e.pad = 0;
+    }
+    return e;
+}
+template <int KW> __device__ __forceinline__ void st_stage(Entry<KW>* p, const Entry<KW>& e, bool global) {
+    if (global) {
+        st_entry(p, e);
+        return;
+    }
+    *reinterpret_cast<uint4*>(p) =
+        make_uint4(uint32_t(e.prio), uint32_t(e.prio >> 32), uint32_t(e.k0), uint32_t(e.k0 >> 32));
+    if constexpr (KW == 2)
+        *(reinterpret_cast<uint4*>(p) + 1) = make_uint4(uint32_t(e.k1), uint32_t(e.k1 >> 32), 0u, 0u);
+}
+
+// ---------------------------------------------------------------------------
+// Warp sorting networks over one entry per lane (ascending by prio).
+// Every compare-exchange decides from the same predicate in both lanes of a
+// pair, so equal priorities never duplicate or drop an entry.
+// ---------------------------------------------------------------------------
+template <int KW> __device__ __forceinline__ Entry<KW> bitonic_clean(Entry<KW> x, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        Entry<KW> y = shfl_xor(x, j);
+        bool lower = !(lane & j);
+        bool sw = lower ? (y.prio < x.prio) : (x.prio < y.prio);
+        if (sw) x = y;
+    }
+    return x;
+}
+
+template <int KW> __device__ __forceinline__ Entry<KW> sort32(Entry<KW> x, int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            Entry<KW> y = shfl_xor(x, j);
+            bool lower = !(lane & j);
+            bool asc = (k == 32) || !(lane & k);
+            bool sw = (lower == asc) ? (y.prio < x.prio) : (x.prio < y.prio);
+            if (sw) x = y;
+        }
+    }
+    return x;
+}
+
+// Merges two ascending 32-entry vectors: lo = 32 smallest, hi = 32 largest,
+// both ascending.
+template <int KW>
+__device__ __forceinline__ void merge2(const Entry<KW>& a, const Entry<KW>& b, Entry<KW>& lo,
+                                       Entry<KW>& hi, int lane) {
+    Entry<KW> br = shfl_idx(b, 31 - lane);
+    bool bl = br.prio < a.prio;
+    lo = bl ? br : a;
+    hi = bl ? a : br;
+    lo = bitonic_clean(lo, lane);
+    hi = bitonic_clean(hi, lane);
+}
+
+// Element idx (0..63) of the concatenation lo ++ hi; all lanes must call.
+template <int KW>
+__device__ __forceinline__ Entry<KW> pick(const Entry<KW>& lo, const Entry<KW>& hi, int idx) {
+    Entry<KW> a = shfl_idx(lo, idx & 31);
+    Entry<KW> b = shfl_idx(hi, idx & 31);
+    return idx < 32 ? a : b;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative batched binary heap.
+//
+// One warp owns one heap.  A node holds 32 entries sorted ascending; the heap
+// order is node-wise (every entry of a node <= every entry of its children),
+// so the root holds the 32 best entries of the tree.  The root node and a
+// partial buffer of < 32 entries live in registers (one entry per lane) for
+// the lifetime of a launch; the other nodes are 512-byte (or 1 KiB) blocks in
+// global memory, read and written with one coalesced access per lane.
+// Replaces the reference's one-thread-per-heap binary heaps with their
+// key->slot index (heaps.h:93-177, device_hashmap.h): stale entries are
+// dropped at pop time instead of being erased (lazy deletion).
+// ---------------------------------------------------------------------------
+template <int KW> struct WarpHeap {
+    Entry<KW>* nodes;  // (cap + 1) * 32 entries; node `cap` stores the saved partial buffer
+    uint32_t* hdr;     // saved {N, pc}
+    uint32_t cap;      // tree nodes available
+    uint32_t N;        // full nodes in the tree (warp-uniform)
+    uint32_t pc;       // entries in the partial buffer (warp-uniform)
+    uint32_t max_n;    // high-water mark of N
+    Entry<KW> root;    // lane l: root[l] (valid iff N > 0)
+    Entry<KW> part;    // lane l: partial[l] (valid iff l < pc), ascending
+};
+
+template <int KW> __device__ __forceinline__ void heap_init(WarpHeap<KW>& h) {
+    h.N = 0;
+    h.pc = 0;
+    h.max_n = 0;
+    h.root = inf_entry<KW>();
+    h.part = inf_entry<KW>();
+}
+
+template <int KW> __device__ __forceinline__ void heap_restore(WarpHeap<KW>& h, int lane) {
+    h.N = __ldcg(h.hdr);
+    h.pc = __ldcg(h.hdr + 1);
+    h.max_n = h.N;
+    h.root = h.N ? ld_entry(h.nodes + lane) : inf_entry<KW>();
+    h.part = (uint32_t)lane < h.pc ? ld_entry(h.nodes + (size_t)h.cap * 32 + lane) : inf_entry<KW>();
+}
+
+template <int KW> __device__ __forceinline__ void heap_save(const WarpHeap<KW>& h, int lane) {
+    if (h.N) st_entry(h.nodes + lane, h.root);
+    st_entry(h.nodes + (size_t)h.cap * 32 + lane, h.part);
+    if (lane == 0) {
+        __stcg(h.hdr, h.N);
+        __stcg(h.hdr + 1, h.pc);
+    }
+}
+
+template <int KW> __device__ __forceinline__ uint64_t heap_min(const WarpHeap<KW>& h) {
+    uint64_t r = __shfl_sync(kFull, h.root.prio, 0);
+    uint64_t p = __shfl_sync(kFull, h.part.prio, 0);
+    r = h.N ? r : kInfPrio;
+    p = h.pc ? p : kInfPrio;
+    return r < p ? r : p;
+}
+
+// Restores the node order below the root after the root's content changed.
+template <int KW> __device__ void heap_sift_down(WarpHeap<KW>& h, int lane) {
+    Entry<KW> cur = h.root;
+    uint32_t idx = 0;
+    for (;;) {
+        uint32_t l = 2 * idx + 1, r = l + 1;
+        if (l >= h.N) break;
+        Entry<KW> L = ld_entry(h.nodes + (size_t)l * 32 + lane);
+        uint64_t cmax = __shfl_sync(kFull, cur.prio, 31);
+        uint64_t lmin = __shfl_sync(kFull, L.prio, 0);
+        if (r >= h.N) {
+            if (cmax > lmin) {
+                Entry<KW> lo, hi;
+                merge2(cur, L, lo, hi, lane);
+                st_entry(h.nodes + (size_t)l * 32 + lane, hi);
+                cur = lo;
+            }
+            break;
+        }
+        Entry<KW> R = ld_entry(h.nodes + (size_t)r * 32 + lane);
+        uint64_t rmin = __shfl_sync(kFull, R.prio, 0);
+        if (cmax <= (lmin < rmin ? lmin : rmin)) break;
+        uint64_t lmax = __shfl_sync(kFull, L.prio, 31);
+        uint64_t rmax = __shfl_sync(kFull, R.prio, 31);
+        Entry<KW> A, B;
+        merge2(L, R, A, B, lane);
+        uint32_t big = lmax >= rmax ? l : r, small = big == l ? r : l;
+        st_entry(h.nodes + (size_t)big * 32 + lane, B);  // B.max = max(lmax, rmax): big's subtree stays ordered
+        Entry<KW> lo, hi;
+        merge2(cur, A, lo, hi, lane);
+        if (idx == 0) h.root = lo;
+        else st_entry(h.nodes + (size_t)idx * 32 + lane, lo);
+        cur = hi;
+        idx = small;
+    }
+    if (idx == 0) h.root = cur;
+    else st_entry(h.nodes + (size_t)idx * 32 + lane, cur);
+}
+
+// Pops the E (1..32) best entries; lane l < return value receives one.
+template <int KW>
+__device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, Entry<KW>& out, int lane) {
+    if (h.N == 0) {
+        uint32_t c = E < h.pc ? E : h.pc;
+        out = (uint32_t)lane < c ? h.part : inf_entry<KW>();
+        Entry<KW> s = shfl_idx(h.part, (lane + (int)c) & 31);
+        h.part = ((uint32_t)lane + c < h.pc) ? s : inf_entry<KW>();
+        h.pc -= c;
+        return c;
+    }
+    Entry<KW> lo, hi;
+    merge2(h.root, h.part, lo, hi, lane);
+    const uint32_t valid = 32 + h.pc, rest = valid - E;
+    out = (uint32_t)lane < E ? lo : inf_entry<KW>();
+    const int i1 = (int)E + lane, i2 = (int)E + 32 + lane;
+    Entry<KW> r1 = pick(lo, hi, i1 & 63);
+    Entry<KW> r2 = pick(lo, hi, i2 & 63);
+    if ((uint32_t)i1 >= valid) r1 = inf_entry<KW>();
+    if ((uint32_t)i2 >= valid) r2 = inf_entry<KW>();
+    if (rest >= 32) {
+        h.root = r1;
+        h.part = r2;
+        h.pc = rest - 32;
+        heap_sift_down(h, lane);
+    } else if (h.N == 1) {
+        h.N = 0;
+        h.root = inf_entry<KW>();
+        h.part = r1;
+        h.pc = rest;
+    } else {
+        Entry<KW> last = ld_entry(h.nodes + (size_t)(h.N - 1) * 32 + lane);
+        h.N -= 1;
+        Entry<KW> lo2, hi2;
+        merge2(last, r1, lo2, hi2, lane);
+        h.root = lo2;
+        h.part = hi2;
+        h.pc = rest;
+        heap_sift_down(h, lane);
+    }
+    return E;
+}
+
+// Adds a full node top-down along the path to the new leaf: every node on the
+// path keeps the 32 smallest of itself and the carried node.
+template <int KW> __device__ bool heap_insert_node(WarpHeap<KW>& h, Entry<KW> F, int lane) {
+    if (h.N == 0) {
+        h.root = F;
+        h.N = 1;
+        if (h.max_n < 1) h.max_n = 1;
+        return true;
+    }
+    if (h.N >= h.cap) return false;
+    const uint32_t p = h.N + 1;
+    const int levels = 31 - __clz(p);
+    {
+        uint64_t fmin = __shfl_sync(kFull, F.prio, 0);
+        uint64_t rmax = __shfl_sync(kFull, h.root.prio, 31);
+        if (fmin < rmax) {
+            Entry<KW> lo, hi;
+            merge2(h.root, F, lo, hi, lane);
+            h.root = lo;
+            F = hi;
+        }
+    }
+    for (int b = levels - 1; b >= 1; --b) {
+        Entry<KW>* np = h.nodes + (size_t)((p >> b) - 1) * 32;
+        uint64_t fmin = __shfl_sync(kFull, F.prio, 0);
+        uint64_t mmax = __ldcg(reinterpret_cast<const unsigned long long*>(&np[31].prio));
+        if (fmin < mmax) {
+            Entry<KW> M = ld_entry(np + lane);
+            Entry<KW> lo, hi;
+            merge2(M, F, lo, hi, lane);
+            st_entry(np + lane, lo);
+            F = hi;
+        }
+    }
+    st_entry(h.nodes + (size_t)h.N * 32 + lane, F);
+    h.N += 1;
+    if (h.N > h.max_n) h.max_n = h.N;
+    return true;
+}
+
+// Pushes up to 32 entries (lanes >= m must hold padding entries).
+template <int KW>
+__device__ bool heap_push(WarpHeap<KW>& h, Entry<KW> x, uint32_t m, int lane) {
+    if (m == 0) return true;
+    x = sort32(x, lane);
+    Entry<KW> lo, hi;
+    merge2(h.part, x, lo, hi, lane);
+    const uint32_t tot = h.pc + m;
+    if (tot < 32) {
+        h.part = lo;
+        h.pc = tot;
+        return true;
+    }
+    // The largest 32 form a new node; the smallest stay in the partial buffer,
+    // where the next pop sees them first.
+    const uint32_t off = tot - 32;
+    Entry<KW> node = pick(lo, hi, (int)off + lane);
+    h.part = (uint32_t)lane < off ? lo : inf_entry<KW>();
+    h.pc = off;
+    return heap_insert_node(h, node, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Duplicate-detection tables.  insert-or-min returns the previous value word;
+// the caller keeps a successor iff its g is strictly below the old g.  This is
+// the reference's NEW -> INSERTED / UPDATED / REJECTED classification
+// (fancy_hashmap.h:32-81, 155-167) as one atomic per successor.
+// ---------------------------------------------------------------------------
+
+// 64-bit keys: slot = {key, value}, 16 bytes; linear probing.
+struct HashTab64 {
+    unsigned long long* s;
+    uint64_t mask;
+    uint32_t max_probe;
+};
+
+// Returns 1 when the key was newly claimed, 0 when found, -1 when full.
+__device__ __forceinline__ int tab_insert(const HashTab64& t, uint64_t key, uint64_t val,
+                                          uint64_t& old) {
+    uint64_t i = mix64(key) & t.mask;
+    for (uint32_t p = 0; p < t.max_probe; ++p) {
+        unsigned long long* ks = t.s + 2 * i;
+        unsigned long long k = __ldcg(ks);
+        int claimed = 0;
+        if (k == kEmpty) {
+            k = atomicCAS(ks, kEmpty, key);
+            if (k == kEmpty) {
+                k = key;
+                claimed = 1;
+            }
+        }
+        if (k == key) {
+            old = atomicMin(ks + 1, val);
+            return claimed;
+        }
+        i = (i + 1) & t.mask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ uint64_t tab_get(const HashTab64& t, uint64_t key) {
+    uint64_t i = mix64(key) & t.mask;
+    for (uint32_t p = 0; p < t.max_probe; ++p) {
+        const unsigned long long* ks = t.s + 2 * i;
+        unsigned long long k = __ldcg(ks);
+        if (k == key) return __ldcg(ks + 1);
+        if (k == kEmpty) return kEmpty;
+        i = (i + 1) & t.mask;
+    }
+    return kEmpty;
+}
+
+// 128-bit keys: slot = {k0, k1, value, pad}, 32 bytes (one sector).  The key
+// is claimed with a 16-byte compare-and-swap; reads of the key pair also go
+// through the 16-byte atomic so a half-written pair is never observed.
+struct HashTab128 {
+    unsigned long long* s;
+    uint64_t mask;
+    uint32_t max_probe;
+};
+
+__device__ __forceinline__ void cas128(unsigned long long* addr, uint64_t c0, uint64_t c1,
+                                       uint64_t n0, uint64_t n1, uint64_t& o0, uint64_t& o1) {
+    asm volatile(
+        "{\n\t.reg .b128 cmp, swp, dst;\n\t"
+        "mov.b128 cmp, {%2, %3};\n\t"
+        "mov.b128 swp, {%4, %5};\n\t"
+        "atom.global.cas.b128 dst, [%6], cmp, swp;\n\t"
+        "mov.b128 {%0, %1}, dst;\n\t}"
+        : "=l"(o0), "=l"(o1)
+        : "l"(c0), "l"(c1), "l"(n0), "l"(n1), "l"(addr)
+        : "memory");
+}
+
+__device__ __forceinline__ uint64_t hash128(uint64_t k0, uint64_t k1) {
+    return mix64(k0 ^ mix64(k1 + 0x9e3779b97f4a7c15ull));
+}
+
+__device__ __forceinline__ int tab_insert(const HashTab128& t, uint64_t k0, uint64_t k1,
+                                          uint64_t val, uint64_t& old) {
+    uint64_t i = hash128(k0, k1) & t.mask;
+    for (uint32_t p = 0; p < t.max_probe; ++p) {
+        unsigned long long* ks = t.s + 4 * i;
+        uint64_t o0, o1;
+        cas128(ks, kEmpty, kEmpty, k0, k1, o0, o1);
+        int claimed = (o0 == kEmpty && o1 == kEmpty);
+        if (claimed || (o0 == k0 && o1 == k1)) {
+            old = atomicMin(ks + 2, val);
+            return claimed;
+        }
+        i = (i + 1) & t.mask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ uint64_t tab_get(const HashTab128& t, uint64_t k0, uint64_t k1) {
+    uint64_t i = hash128(k0, k1) & t.mask;
+    for (uint32_t p = 0; p < t.max_probe; ++p) {
+        unsigned long long* ks = t.s + 4 * i;
+        uint64_t o0, o1;
+        cas128(ks, kEmpty, kEmpty, kEmpty, kEmpty, o0, o1);  // atomic 16-byte read
+        if (o0 == k0 && o1 == k1) return __ldcg(ks + 2);
+        if (o0 == kEmpty && o1 == kEmpty) return kEmpty;
+        i = (i + 1) & t.mask;
+    }
+    return kEmpty;
+}
+
+// Dense table for grids: the cell index is the slot (a perfect hash).
+struct DenseTab {
+    unsigned long long* v;
+};
+
+}  // namespace gastar

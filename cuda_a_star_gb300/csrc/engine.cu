@@ -1,0 +1,628 @@
+// Host runtime and C ABI of the GA* engine (libgastar.so).
+//
+// Plain mode  : one instance per launch; a team of thread blocks (cooperative
+//               launch, device-side barriers) runs the whole search without a
+//               host round trip.  Replaces a_star() (a_star.h:223-282).
+// Batch mode  : many instances in one persistent launch, one block per
+//               instance at a time, per-instance table/heap partitions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gastar.h"
+#include "engine_internal.h"
+#include "search.cuh"
+
+namespace gastar {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& s) { g_last_error = s; }
+
+bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    return false;
+}
+
+#define GA_CUDA(call)                                  \
+    do {                                               \
+        if (!cuda_ok((call), #call)) return GASTAR_CUDA_ERROR; \
+    } while (0)
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+}
+
+bool DevBuf::ensure(size_t bytes) {
+    if (bytes <= n) return true;
+    release();
+    size_t want = bytes < 256 ? 256 : bytes;
+    if (!cuda_ok(cudaMalloc(&p, want), "cudaMalloc")) {
+        p = nullptr;
+        return false;
+    }
+    n = want;
+    return true;
+}
+
+template <uint32_t K> const void* kernel_ptr() { return reinterpret_cast<const void*>(&search_kernel<K>); }
+
+const void* search_kernel_for(uint32_t kinds) {
+    switch (kinds) {
+        case kind_bit(KIND_SLIDING3): return kernel_ptr<kind_bit(KIND_SLIDING3)>();
+        case kind_bit(KIND_SLIDING4): return kernel_ptr<kind_bit(KIND_SLIDING4)>();
+        case kind_bit(KIND_SLIDING5): return kernel_ptr<kind_bit(KIND_SLIDING5)>();
+        case kind_bit(KIND_GRID): return kernel_ptr<kind_bit(KIND_GRID)>();
+        default: return kernel_ptr<kKindsAll>();
+    }
+}
+
+uint32_t entry_bytes(uint32_t kind) { return kind == KIND_SLIDING5 ? 32u : 16u; }
+uint32_t max_neighbours(uint32_t kind) { return kind == KIND_GRID ? 8u : 4u; }
+uint32_t key_words(uint32_t kind) { return kind == KIND_SLIDING5 ? 2u : 1u; }
+
+size_t stage_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew) {
+    size_t best = 0;
+    for (uint32_t k = 0; k < 4; ++k)
+        if (kinds & kind_bit(k))
+            best = std::max(best, (size_t)warps * ew * max_neighbours(k) * entry_bytes(k));
+    return best;
+}
+
+int occupancy_blocks(gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem) {
+    const void* f = search_kernel_for(kinds);
+    if (smem > 48 * 1024)
+        if (!cuda_ok(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                     "cudaFuncSetAttribute"))
+            return 0;
+    int nb = 0;
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, (int)threads, smem),
+                 "cudaOccupancyMaxActiveBlocksPerMultiprocessor"))
+        return 0;
+    return nb;
+}
+
+int launch_search(gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
+                  uint32_t threads, size_t smem, cudaStream_t st) {
+    const void* f = search_kernel_for(kinds);
+    if (smem > 48 * 1024)
+        GA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    LaunchParams p = P;
+    void* args[] = {&p};
+    if (P.team_ctas > 1) {
+        GA_CUDA(cudaLaunchCooperativeKernel(f, dim3(blocks), dim3(threads), args, smem, st));
+    } else {
+        GA_CUDA(cudaLaunchKernel(f, dim3(blocks), dim3(threads), args, smem, st));
+    }
+    return GASTAR_OK;
+}
+
+int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
+                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st) {
+    const uint32_t t = 64;
+    path_kernel<<<(n + t - 1) / t, t, 0, st>>>(d_insts, n, arena, arena_words, used);
+    GA_CUDA(cudaGetLastError());
+    return GASTAR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Problem encoding on the host.
+// ---------------------------------------------------------------------------
+bool valid_board(uint32_t n, const uint8_t* b) {
+    if (n < 3 || n > 5 || !b) return false;
+    uint32_t seen = 0;
+    for (uint32_t i = 0; i < n * n; ++i) {
+        if (b[i] >= n * n || (seen >> b[i]) & 1u) return false;
+        seen |= 1u << b[i];
+    }
+    return true;
+}
+
+void pack_board(uint32_t n, const uint8_t* b, uint64_t& lo, uint64_t& hi) {
+    const uint32_t B = n <= 4 ? 4 : 5;
+    unsigned __int128 k = 0;
+    for (uint32_t i = 0; i < n * n; ++i) k |= (unsigned __int128)b[i] << (B * i);
+    lo = (uint64_t)k;
+    hi = (uint64_t)(k >> 64);
+}
+
+void unpack_board(uint32_t n, uint64_t lo, uint64_t hi, uint8_t* b) {
+    const uint32_t B = n <= 4 ? 4 : 5;
+    const unsigned __int128 k = ((unsigned __int128)hi << 64) | lo;
+    for (uint32_t i = 0; i < n * n; ++i) b[i] = (uint8_t)((k >> (B * i)) & ((1u << B) - 1));
+}
+
+uint32_t sliding_h(uint32_t n, const uint8_t* b, const uint8_t* goal, uint32_t heuristic) {
+    if (heuristic == GASTAR_H_ZERO) return 0;
+    int gr[32], gc[32];
+    for (uint32_t i = 0; i < n * n; ++i) {
+        gr[goal[i]] = (int)(i / n);
+        gc[goal[i]] = (int)(i % n);
+    }
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < n * n; ++i) {
+        if (b[i] == 0 && heuristic != GASTAR_H_REFERENCE) continue;
+        s += (uint32_t)(std::abs(gr[b[i]] - (int)(i / n)) + std::abs(gc[b[i]] - (int)(i % n)));
+    }
+    return s;
+}
+
+bool sliding_solvable(uint32_t n, const uint8_t* s, const uint8_t* g) {
+    auto inv = [n](const uint8_t* b) {
+        uint32_t c = 0, blank = 0;
+        for (uint32_t i = 0; i < n * n; ++i) {
+            if (!b[i]) {
+                blank = i;
+                continue;
+            }
+            for (uint32_t j = i + 1; j < n * n; ++j)
+                if (b[j] && b[j] < b[i]) ++c;
+        }
+        if ((n & 1) == 0) c += blank / n;
+        return c & 1u;
+    };
+    return inv(s) == inv(g);
+}
+
+uint32_t grid_h(uint32_t x, uint32_t y, uint32_t tx, uint32_t ty, uint32_t minw, uint32_t heuristic) {
+    const uint32_t ax = x > tx ? x - tx : tx - x, ay = y > ty ? y - ty : ty - y;
+    if (heuristic == GASTAR_H_REFERENCE) return ax + ay;
+    if (heuristic == GASTAR_H_ZERO) return 0;
+    return std::max(ax, ay) * minw;
+}
+
+uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+}  // namespace gastar
+
+using namespace gastar;
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gastar_version(void) { return 100; }
+
+const char* gastar_last_error(void) { return g_last_error.c_str(); }
+
+const char* gastar_status_name(int s) {
+    static const char* names[] = {"OK", "NO_PATH", "BUDGET", "TIMEOUT", "HEAP_FULL", "TABLE_FULL",
+                                  "PATH_CAP", "BARRIER_TIMEOUT", "BAD_INPUT", "CUDA_ERROR",
+                                  "NO_DEVICE", "PENDING", "OUT_OF_MEMORY"};
+    if (s < 0 || s >= (int)(sizeof(names) / sizeof(names[0]))) return "UNKNOWN";
+    return names[s];
+}
+
+void gastar_config_default(gastar_config* cfg) {
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->num_queues = 4096;
+    cfg->heuristic = GASTAR_H_ADMISSIBLE;
+    cfg->moves = GASTAR_MOVES_STANDARD;
+    cfg->expansion_width = 32;
+    cfg->warps_per_block = 4;
+    cfg->load_factor = 0.75f;
+    cfg->regrow = 1;
+}
+
+gastar_ctx* gastar_create(int device) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        set_error("no CUDA device");
+        return nullptr;
+    }
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) device = 0;
+    if (device >= count) {
+        set_error("device index out of range");
+        return nullptr;
+    }
+    if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice")) return nullptr;
+    auto* c = new gastar_ctx();
+    c->device = device;
+    cudaDeviceProp prop;
+    if (!cuda_ok(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties")) {
+        delete c;
+        return nullptr;
+    }
+    c->sms = prop.multiProcessorCount;
+    c->mem_total = prop.totalGlobalMem;
+    std::snprintf(c->name, sizeof(c->name), "%s", prop.name);
+    c->coop = prop.cooperativeLaunch;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaEventCreate(&c->e0), "cudaEventCreate") ||
+        !cuda_ok(cudaEventCreate(&c->e1), "cudaEventCreate") ||
+        !cuda_ok(cudaMallocHost(&c->h_ctl, sizeof(InstCtl)), "cudaMallocHost")) {
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+
+void gastar_destroy(gastar_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->table.release();
+    c->heaps.release();
+    c->hdr.release();
+    c->stage.release();
+    c->desc.release();
+    c->ctl.release();
+    c->team.release();
+    c->path.release();
+    c->misc.release();
+    c->weights.release();
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->e0) cudaEventDestroy(c->e0);
+    if (c->e1) cudaEventDestroy(c->e1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int gastar_device_info(gastar_ctx* c, int* sm_count, uint64_t* mem_bytes, char* name, size_t name_len) {
+    if (!c) return GASTAR_BAD_INPUT;
+    if (sm_count) *sm_count = c->sms;
+    if (mem_bytes) *mem_bytes = c->mem_total;
+    if (name && name_len) std::snprintf(name, name_len, "%s", c->name);
+    return GASTAR_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Plain engine
+// ---------------------------------------------------------------------------
+namespace gastar {
+
+struct PlainProblem {
+    uint32_t kind, n;
+    uint64_t start0, start1, goal0, goal1;
+    const uint8_t* d_weights;  // grid (device)
+    uint32_t W, H, minw, f0;
+};
+
+static void fill_result(gastar_result* out, const InstCtl& c) {
+    out->status = (int32_t)c.status;
+    out->cost = c.status == ST_OK || c.status == ST_PATH_CAP ? c.best : 0;
+    out->path_len = c.path_len;
+    out->iterations = c.iterations;
+    out->expansions = c.expansions;
+    out->generated = c.generated;
+    out->pushes = c.pushes;
+    out->stale = c.stale;
+    out->table_used = c.table_used;
+}
+
+// Runs the search (+ path rebuild) once with the given capacities.
+static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_config& cfg,
+                         uint32_t table_log2, uint64_t heap_entries, bool want_path,
+                         cudaStream_t st, InstCtl& ctl_out, float& kernel_ms) {
+    const uint32_t kinds = kind_bit(pp.kind);
+    const uint32_t ew = std::min(32u, std::max(1u, cfg.expansion_width ? cfg.expansion_width : 32u));
+    const uint32_t W = std::min(16u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
+    const uint32_t threads = W * 32;
+    const uint64_t Q = cfg.num_queues ? cfg.num_queues : 4096;
+    uint64_t heaps = (Q + ew - 1) / ew;
+    uint64_t blocks = (heaps + W - 1) / W;
+    const bool multi = blocks > 1;
+    const size_t smem = multi ? 0 : stage_smem_bytes(kinds, W, ew);
+    const int nb = occupancy_blocks(c, kinds, threads, smem);
+    if (nb <= 0) return GASTAR_CUDA_ERROR;
+    uint64_t max_blocks = (uint64_t)nb * c->sms;
+    if (cfg.max_blocks) max_blocks = std::min<uint64_t>(max_blocks, cfg.max_blocks);
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (multi && !c->coop) {
+        set_error("device does not support cooperative launch");
+        return GASTAR_CUDA_ERROR;
+    }
+    heaps = blocks * W;
+
+    // Table.
+    const uint32_t ebytes = entry_bytes(pp.kind), kw = key_words(pp.kind);
+    uint64_t table_words, mask = 0, limit;
+    if (pp.kind == KIND_GRID) {
+        table_words = (uint64_t)pp.W * pp.H;
+        limit = ~0ull;
+    } else {
+        const uint64_t slots = 1ull << table_log2;
+        table_words = slots * (kw == 1 ? 2 : 4);
+        mask = slots - 1;
+        float lf = cfg.load_factor > 0.f ? cfg.load_factor : 0.75f;
+        lf = std::min(0.95f, std::max(0.1f, lf));
+        limit = (uint64_t)((double)slots * lf);
+    }
+    // Heaps: per warp-heap node capacity with headroom for uneven dealing.
+    uint64_t per_heap = (heap_entries + heaps - 1) / heaps;
+    uint64_t cap_nodes = std::max<uint64_t>(4, (per_heap * 2 + 31) / 32);
+    if (cap_nodes > 0x7fffffffull) return GASTAR_OUT_OF_MEMORY;
+    const size_t heap_bytes = (size_t)heaps * (cap_nodes + 1) * 32 * ebytes;
+    const size_t stage_entries = multi ? (size_t)heaps * ew * max_neighbours(pp.kind) : 0;
+
+    if (!c->table.ensure(table_words * 8) || !c->heaps.ensure(heap_bytes) ||
+        !c->hdr.ensure((size_t)heaps * 8) || !c->stage.ensure(std::max<size_t>(stage_entries * ebytes, 16)) ||
+        !c->desc.ensure(sizeof(InstDesc)) || !c->ctl.ensure(sizeof(InstCtl)) ||
+        !c->team.ensure(sizeof(TeamCtl) + 64))
+        return GASTAR_OUT_OF_MEMORY;
+
+    InstDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.kind = pp.kind;
+    d.heuristic = cfg.heuristic;
+    d.moves = cfg.moves;
+    d.n = pp.n;
+    d.start0 = pp.start0;
+    d.start1 = pp.start1;
+    d.goal0 = pp.goal0;
+    d.goal1 = pp.goal1;
+    d.weights = pp.d_weights;
+    d.W = pp.W;
+    d.H = pp.H;
+    d.minw = pp.minw;
+    d.f0 = pp.f0;
+    d.table = reinterpret_cast<unsigned long long*>(c->table.p);
+    d.table_words = table_words;
+    d.table_mask = mask;
+    d.table_limit = limit;
+    d.max_probe = 4096;
+    d.heaps = (uint32_t)heaps;
+    d.heap_nodes = c->heaps.p;
+    d.heap_hdr = reinterpret_cast<uint32_t*>(c->hdr.p);
+    d.heap_cap = (uint32_t)cap_nodes;
+    d.ew = ew;
+    d.max_exp = cfg.max_expansions;
+    d.timeout_ns = (uint64_t)cfg.timeout_ms * 1000000ull;
+    d.max_iter = cfg.max_iterations;
+    d.ctl = reinterpret_cast<InstCtl*>(c->ctl.p);
+    c->h_desc = d;
+
+    TeamCtl tc;
+    std::memset(&tc, 0, sizeof(tc));
+    for (auto& s : tc.slot) {
+        s.minprio = ~0ull;
+        s.best = kInf;
+    }
+    c->h_team = tc;
+
+    LaunchParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.insts = reinterpret_cast<const InstDesc*>(c->desc.p);
+    P.n_insts = 1;
+    P.next = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(c->team.p) + sizeof(TeamCtl));
+    P.team_ctas = (uint32_t)blocks;
+    P.team = reinterpret_cast<TeamCtl*>(c->team.p);
+    P.stage = c->stage.p;
+    P.barrier_timeout_ns = 2000000000ull;
+
+    GA_CUDA(cudaMemcpyAsync(c->desc.p, &c->h_desc, sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+    GA_CUDA(cudaMemsetAsync(c->ctl.p, 0, sizeof(InstCtl), st));
+    GA_CUDA(cudaMemcpyAsync(c->team.p, &c->h_team, sizeof(TeamCtl), cudaMemcpyHostToDevice, st));
+    GA_CUDA(cudaMemsetAsync(P.next, 0, 16, st));
+    GA_CUDA(cudaEventRecord(c->e0, st));
+    int rc = launch_search(c, kinds, P, (uint32_t)blocks, threads, smem, st);
+    if (rc != GASTAR_OK) return rc;
+    GA_CUDA(cudaEventRecord(c->e1, st));
+    if (want_path) {
+        // Arena: best + 1 states is the longest possible path; size it after
+        // reading best would need a round trip, so reserve by kind.
+        GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
+        GA_CUDA(cudaStreamSynchronize(st));
+        if (c->h_ctl->status == ST_OK) {
+            const uint64_t words = ((uint64_t)c->h_ctl->best + 2) * kw;
+            if (!c->path.ensure(words * 8 + 16)) return GASTAR_OUT_OF_MEMORY;
+            if (!c->misc.ensure(16)) return GASTAR_OUT_OF_MEMORY;
+            GA_CUDA(cudaMemsetAsync(c->misc.p, 0, 16, st));
+            rc = launch_paths(reinterpret_cast<const InstDesc*>(c->desc.p), 1,
+                              reinterpret_cast<unsigned long long*>(c->path.p), words,
+                              reinterpret_cast<unsigned long long*>(c->misc.p), st);
+            if (rc != GASTAR_OK) return rc;
+        }
+    }
+    GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
+    GA_CUDA(cudaStreamSynchronize(st));
+    GA_CUDA(cudaEventElapsedTime(&kernel_ms, c->e0, c->e1));
+    ctl_out = *c->h_ctl;
+    return GASTAR_OK;
+}
+
+int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user_cfg,
+                std::vector<uint64_t>* path_keys, gastar_result* out) {
+    gastar_config cfg;
+    if (user_cfg) cfg = *user_cfg;
+    else gastar_config_default(&cfg);
+    cudaStream_t st = cfg.stream ? (cudaStream_t)cfg.stream : c->stream;
+    uint32_t table_log2 = cfg.table_log2;
+    const uint32_t max_log2 = pp.kind == KIND_SLIDING5 ? 29 : 30;
+    if (!table_log2) table_log2 = pp.kind == KIND_SLIDING3 ? 19 : 22;
+    table_log2 = std::min(table_log2, max_log2);
+    uint64_t heap_entries = cfg.heap_entries;
+    if (!heap_entries)
+        heap_entries = pp.kind == KIND_GRID ? std::max<uint64_t>(1 << 20, (uint64_t)pp.W * pp.H)
+                                            : (1ull << table_log2);
+    InstCtl ctl;
+    float ms = 0;
+    float total_ms = 0;
+    uint32_t attempts = 0;
+    for (;;) {
+        ++attempts;
+        int rc = plain_attempt(c, pp, cfg, table_log2, heap_entries, path_keys != nullptr, st, ctl, ms);
+        if (rc != GASTAR_OK) return rc;
+        total_ms += ms;
+        if (!cfg.regrow && user_cfg) break;
+        if (ctl.status == ST_TABLE_FULL && pp.kind != KIND_GRID && table_log2 < max_log2) {
+            ++table_log2;
+            heap_entries = std::max<uint64_t>(heap_entries, 1ull << table_log2);
+            continue;
+        }
+        if (ctl.status == ST_HEAP_FULL && heap_entries < (1ull << 32)) {
+            heap_entries *= 2;
+            continue;
+        }
+        break;
+    }
+    fill_result(out, ctl);
+    out->kernel_ms = total_ms;
+    out->attempts = attempts;
+    if (path_keys && ctl.status == ST_OK) {
+        const uint32_t kw = key_words(pp.kind);
+        path_keys->resize((size_t)ctl.path_len * kw);
+        GA_CUDA(cudaMemcpyAsync(path_keys->data(),
+                                reinterpret_cast<unsigned long long*>(c->path.p) + ctl.path_off,
+                                path_keys->size() * 8, cudaMemcpyDeviceToHost, st));
+        GA_CUDA(cudaStreamSynchronize(st));
+    }
+    return GASTAR_OK;
+}
+
+}  // namespace gastar
+
+extern "C" {
+
+int gastar_solve_sliding(gastar_ctx* c, uint32_t n, const uint8_t* start, const uint8_t* goal,
+                         const gastar_config* cfg, uint8_t* path, uint32_t path_cap,
+                         gastar_result* out) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!c || !out) return GASTAR_BAD_INPUT;
+    std::memset(out, 0, sizeof(*out));
+    if (!valid_board(n, start) || !valid_board(n, goal)) {
+        set_error("sliding: boards must be permutations of 0..n*n-1 with n in 3..5");
+        out->status = GASTAR_BAD_INPUT;
+        return GASTAR_BAD_INPUT;
+    }
+    gastar_config dc;
+    gastar_config_default(&dc);
+    const gastar_config& cf = cfg ? *cfg : dc;
+    if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
+    // The standard four-move puzzle splits into two parity classes; a goal in
+    // the other class is unreachable, so there is no search to run.
+    if (cf.moves == GASTAR_MOVES_STANDARD && !sliding_solvable(n, start, goal)) {
+        out->status = GASTAR_NO_PATH;
+        out->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return GASTAR_OK;
+    }
+    PlainProblem pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.kind = n == 3 ? KIND_SLIDING3 : n == 4 ? KIND_SLIDING4 : KIND_SLIDING5;
+    pp.n = n;
+    pack_board(n, start, pp.start0, pp.start1);
+    pack_board(n, goal, pp.goal0, pp.goal1);
+    pp.f0 = sliding_h(n, start, goal, cf.heuristic);
+    std::vector<uint64_t> keys;
+    int rc = plain_solve(c, pp, cfg, path ? &keys : nullptr, out);
+    if (rc != GASTAR_OK) {
+        out->status = rc;
+        return rc;
+    }
+    if (path && out->status == GASTAR_OK) {
+        const uint32_t kw = key_words(pp.kind);
+        if (out->path_len > path_cap) {
+            out->status = GASTAR_PATH_CAP;
+        } else {
+            for (uint32_t i = 0; i < out->path_len; ++i) {  // stored goal-first
+                const uint32_t j = out->path_len - 1 - i;
+                unpack_board(n, keys[(size_t)j * kw], kw == 2 ? keys[(size_t)j * kw + 1] : 0,
+                             path + (size_t)i * n * n);
+            }
+        }
+    }
+    out->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return GASTAR_OK;
+}
+
+static int solve_grid_impl(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* d_weights,
+                           uint32_t minw, uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty,
+                           const gastar_config* cfg, uint32_t* path, uint32_t path_cap,
+                           gastar_result* out, std::chrono::steady_clock::time_point t0) {
+    gastar_config dc;
+    gastar_config_default(&dc);
+    const gastar_config& cf = cfg ? *cfg : dc;
+    PlainProblem pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.kind = KIND_GRID;
+    pp.start0 = (uint64_t)sy * w + sx;
+    pp.goal0 = (uint64_t)ty * w + tx;
+    pp.d_weights = d_weights;
+    pp.W = w;
+    pp.H = h;
+    pp.minw = minw;
+    pp.f0 = grid_h(sx, sy, tx, ty, minw, cf.heuristic);
+    std::vector<uint64_t> keys;
+    int rc = plain_solve(c, pp, cfg, path ? &keys : nullptr, out);
+    if (rc != GASTAR_OK) {
+        out->status = rc;
+        return rc;
+    }
+    if (path && out->status == GASTAR_OK) {
+        if (out->path_len > path_cap) out->status = GASTAR_PATH_CAP;
+        else
+            for (uint32_t i = 0; i < out->path_len; ++i) path[i] = (uint32_t)keys[out->path_len - 1 - i];
+    }
+    out->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return GASTAR_OK;
+}
+
+static bool grid_args_ok(uint32_t w, uint32_t h, uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty) {
+    return w && h && w <= 65535 && h <= 65535 && (uint64_t)w * h < (1ull << 32) && sx < w && sy < h &&
+           tx < w && ty < h;
+}
+
+int gastar_solve_grid(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx,
+                      uint32_t sy, uint32_t tx, uint32_t ty, const gastar_config* cfg,
+                      uint32_t* path, uint32_t path_cap, gastar_result* out) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!c || !out) return GASTAR_BAD_INPUT;
+    std::memset(out, 0, sizeof(*out));
+    if (!weights || !grid_args_ok(w, h, sx, sy, tx, ty)) {
+        set_error("grid: bad dimensions or endpoints");
+        out->status = GASTAR_BAD_INPUT;
+        return GASTAR_BAD_INPUT;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
+    const size_t cells = (size_t)w * h;
+    uint32_t minw = 255;
+    for (size_t i = 0; i < cells; ++i)
+        if (weights[i] && weights[i] < minw) minw = weights[i];
+    gastar_config dc;
+    gastar_config_default(&dc);
+    cudaStream_t st = (cfg && cfg->stream) ? (cudaStream_t)cfg->stream : c->stream;
+    if (!c->weights.ensure(cells)) return GASTAR_OUT_OF_MEMORY;
+    if (!cuda_ok(cudaMemcpyAsync(c->weights.p, weights, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+        return GASTAR_CUDA_ERROR;
+    return solve_grid_impl(c, w, h, reinterpret_cast<const uint8_t*>(c->weights.p), minw, sx, sy, tx,
+                           ty, cfg, path, path_cap, out, t0);
+}
+
+int gastar_solve_grid_device(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* d_weights,
+                             uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty,
+                             const gastar_config* cfg, uint32_t* path, uint32_t path_cap,
+                             gastar_result* out) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!c || !out) return GASTAR_BAD_INPUT;
+    std::memset(out, 0, sizeof(*out));
+    if (!d_weights || !grid_args_ok(w, h, sx, sy, tx, ty)) {
+        set_error("grid: bad dimensions or endpoints");
+        out->status = GASTAR_BAD_INPUT;
+        return GASTAR_BAD_INPUT;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
+    cudaStream_t st = (cfg && cfg->stream) ? (cudaStream_t)cfg->stream : c->stream;
+    uint32_t minw = 1;
+    int rc = device_min_weight(c, d_weights, (uint64_t)w * h, st, &minw);
+    if (rc != GASTAR_OK) return rc;
+    return solve_grid_impl(c, w, h, d_weights, minw, sx, sy, tx, ty, cfg, path, path_cap, out, t0);
+}
+
+}  // extern "C"

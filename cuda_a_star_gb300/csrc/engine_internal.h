@@ -1,0 +1,60 @@
+// Internal host-side declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gastar.h"
+#include "engine_types.h"
+
+namespace gastar {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    bool ensure(size_t bytes);  // grows (contents are not kept)
+    void release();
+};
+
+void set_error(const std::string& s);
+bool cuda_ok(cudaError_t e, const char* what);
+
+const void* search_kernel_for(uint32_t kinds);
+uint32_t entry_bytes(uint32_t kind);
+uint32_t max_neighbours(uint32_t kind);
+uint32_t key_words(uint32_t kind);
+size_t stage_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew);
+int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
+                  uint32_t threads, size_t smem, cudaStream_t st);
+int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
+                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st);
+int occupancy_blocks(struct ::gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem);
+int device_min_weight(struct ::gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStream_t st,
+                      uint32_t* out);
+
+bool valid_board(uint32_t n, const uint8_t* b);
+void pack_board(uint32_t n, const uint8_t* b, uint64_t& lo, uint64_t& hi);
+void unpack_board(uint32_t n, uint64_t lo, uint64_t hi, uint8_t* b);
+uint32_t sliding_h(uint32_t n, const uint8_t* b, const uint8_t* goal, uint32_t heuristic);
+bool sliding_solvable(uint32_t n, const uint8_t* s, const uint8_t* g);
+uint32_t grid_h(uint32_t x, uint32_t y, uint32_t tx, uint32_t ty, uint32_t minw, uint32_t heuristic);
+uint64_t next_pow2(uint64_t v);
+
+}  // namespace gastar
+
+struct gastar_ctx {
+    int device = 0;
+    int sms = 0;
+    int coop = 0;
+    size_t mem_total = 0;
+    char name[256] = {0};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    gastar::DevBuf table, heaps, hdr, stage, desc, ctl, team, path, misc, weights;
+    gastar::InstCtl* h_ctl = nullptr;  // pinned
+    gastar::InstDesc h_desc;
+    gastar::TeamCtl h_team;
+};

@@ -1,0 +1,74 @@
+// Host/device shared descriptors of the GA* engine.
+#pragma once
+
+#include <cstdint>
+
+namespace gastar {
+
+// Problem kinds compiled into the search kernel.
+enum Kind : uint32_t { KIND_SLIDING3 = 0, KIND_SLIDING4 = 1, KIND_SLIDING5 = 2, KIND_GRID = 3 };
+constexpr uint32_t kKindsAll = 0xf;
+constexpr uint32_t kind_bit(uint32_t k) { return 1u << k; }
+
+// Per-instance control block, written by the device.
+struct alignas(16) InstCtl {
+    uint32_t life;        // LIFE_FRESH / LIFE_RUNNING / LIFE_DONE
+    uint32_t status;      // gastar_status of the finished search
+    uint32_t best;        // best goal cost found (0xffffffff = none)
+    uint32_t iterations;  // GA* iterations run so far
+    uint32_t path_len;    // states on the rebuilt path
+    uint32_t max_nodes;   // largest warp-heap size seen (32-entry nodes)
+    uint64_t t_start;     // device globaltimer at the first iteration
+    unsigned long long expansions, generated, pushes, stale, table_used;
+    unsigned long long path_off;  // offset (64-bit words) of the path in the path arena
+    unsigned long long pad;
+};
+
+// Per-instance description, written by the host.
+struct alignas(16) InstDesc {
+    uint32_t kind, heuristic, moves, n;
+    uint64_t start0, start1, goal0, goal1;  // packed keys (grid: cell index in start0/goal0)
+    const uint8_t* weights;                 // grid: device pointer, w*h bytes
+    uint32_t W, H, minw, f0;                // grid dims, minimum weight; f of the start
+    unsigned long long* table;              // hash slots or dense value array
+    uint64_t table_words;                   // 64-bit words in the table region
+    uint64_t table_mask;                    // slots - 1 (hash tables)
+    uint64_t table_limit;                   // claimed-slot limit before TABLE_FULL
+    uint32_t max_probe, heaps;              // probe limit; warp-heaps of the instance
+    void* heap_nodes;                       // heaps * (heap_cap + 1) * 32 entries
+    uint32_t* heap_hdr;                     // heaps * 2 words
+    uint32_t heap_cap, ew;                  // nodes per warp-heap; pops per heap per iteration
+    uint64_t max_exp;                       // expansion budget (0 = none)
+    uint64_t timeout_ns;                    // device deadline relative to t_start (0 = none)
+    uint32_t max_iter, pad0;                // iteration budget
+    InstCtl* ctl;
+};
+
+struct alignas(16) TeamSlot {
+    unsigned long long minprio;  // min priority over the team's heaps after the push phase
+    uint32_t count;              // entries staged in the pop/expand phase
+    uint32_t best;               // goal costs found in the pop/expand phase
+    uint32_t err;                // first error raised in the iteration
+    uint32_t pad[3];
+};
+
+// Control of a multi-block team (one instance on many blocks).
+struct alignas(16) TeamCtl {
+    uint32_t arrive, gen, abort, pad;
+    TeamSlot slot[3];
+};
+
+struct LaunchParams {
+    const InstDesc* insts;
+    uint32_t n_insts;
+    uint32_t slice_iters;     // 0 = run each instance to completion
+    const uint32_t* order;    // schedule order (nullptr = 0..n-1)
+    uint32_t* next;           // work counter for single-block teams
+    uint32_t team_ctas;       // 1 = one block per instance; >1 = all blocks on instance 0
+    uint32_t pad;
+    TeamCtl* team;            // multi-block team control (device)
+    void* stage;              // multi-block stage buffer (device)
+    uint64_t barrier_timeout_ns;
+};
+
+}  // namespace gastar

@@ -1,0 +1,655 @@
+// The GA* search: problem domains and the persistent search kernel.
+//
+// One "team" of thread blocks works on one instance; each warp of the team
+// owns one warp-heap.  An iteration is
+//   pop    : every warp pops up to `ew` best entries (one per lane), drops
+//            stale ones (table g lower than the entry's g) and goal states;
+//   expand : every lane generates the successors of its entry, computes g and
+//            an incrementally updated h, and does one insert-or-min on the
+//            duplicate-detection table per successor; improved successors go
+//            to the team's stage buffer (shared memory for one-block teams);
+//   push   : after a team barrier, stage chunks are dealt round-robin (with a
+//            rotating offset) to the warp-heaps, which push them;
+//   check  : the team's minimum priority is reduced; the search ends when the
+//            best goal cost is <= min f over all open entries.
+// This is the reference's iteration (a_star.h:247-264: extract_nodes, three
+// bitonic sorts, mark_duplicates, insert_unique_data, remove_updated_elements,
+// insert_nodes_into_queues, two host reductions) as one device-resident loop
+// with two barriers and no host round trip.
+#pragma once
+
+#include <type_traits>
+
+#include "device_common.cuh"
+#include "engine_types.h"
+
+namespace gastar {
+
+// ---------------------------------------------------------------------------
+// Sliding puzzle, n x n.  Keys pack the tile of cell i in bits [B*i, B*i+B)
+// (B = 4 for n <= 4 in a uint64, B = 5 for n = 5 in 128 bits).  Moves follow
+// the reference's neighbour_generator (a_star_sliding_puzzle.h:84-123):
+// move 0/1/2/3 moves the blank row+1 / row-1 / col+1 / col-1, cost 1.
+// ---------------------------------------------------------------------------
+template <int N> struct SlidingDom {
+    static constexpr int KW = N <= 4 ? 1 : 2;
+    static constexpr int MAXN = 4;
+    static constexpr int B = N <= 4 ? 4 : 5;
+    static constexpr int C = N * N;
+    using KeyT = std::conditional_t<KW == 1, uint64_t, unsigned __int128>;
+    using Tab = std::conditional_t<KW == 1, HashTab64, HashTab128>;
+    using Pre = int;  // blank cell
+
+    struct Ctx {
+        KeyT goal, start;
+        uint32_t ref_h, ref_moves;
+        uint8_t md[C][C];  // md[t][p]: Manhattan distance of tile t placed at cell p
+    };
+
+    static __device__ __forceinline__ uint32_t field(KeyT k, int i) {
+        return uint32_t(k >> (B * i)) & ((1u << B) - 1);
+    }
+    static __device__ __forceinline__ KeyT key_of(const Entry<KW>& e) {
+        if constexpr (KW == 1) return e.k0;
+        else return (KeyT(e.k1) << 64) | KeyT(e.k0);
+    }
+    static __device__ __forceinline__ void set_key(Entry<KW>& e, KeyT k) {
+        e.k0 = uint64_t(k);
+        if constexpr (KW == 2) e.k1 = uint64_t(k >> 64);
+    }
+    static __device__ __forceinline__ KeyT desc_key(uint64_t lo, uint64_t hi) {
+        if constexpr (KW == 1) return lo;
+        else return (KeyT(hi) << 64) | KeyT(lo);
+    }
+
+    // Cell of the blank: the unique all-zero field, found with an AND-fold of
+    // the complemented key.
+    static __device__ __forceinline__ int blank_of(KeyT k) {
+        KeyT y = ~k;
+        KeyT z = y & (y >> 1);
+        z = z & (z >> 2);
+        if constexpr (B == 5) z = z & (y >> 4);
+        KeyT mask = 0;
+#pragma unroll
+        for (int i = 0; i < C; ++i) mask |= KeyT(1) << (B * i);
+        z &= mask;
+        if constexpr (KW == 1) {
+            return (__ffsll((long long)z) - 1) / B;
+        } else {
+            uint64_t lo = uint64_t(z), hi = uint64_t(z >> 64);
+            int bit = lo ? __ffsll((long long)lo) - 1 : 64 + __ffsll((long long)hi) - 1;
+            return bit / B;
+        }
+    }
+
+    static __device__ void load(Ctx& c, const InstDesc& d) {
+        const KeyT goal = desc_key(d.goal0, d.goal1);
+        for (int i = threadIdx.x; i < C * C; i += blockDim.x) {
+            const int t = i / C, p = i % C;
+            int gp = 0;
+            for (int q = 0; q < C; ++q)
+                if ((int)field(goal, q) == t) gp = q;
+            int v = abs(gp / N - p / N) + abs(gp % N - p % N);
+            c.md[t][p] = d.heuristic == 2 ? 0 : (uint8_t)v;
+        }
+        if (threadIdx.x == 0) {
+            c.goal = goal;
+            c.start = desc_key(d.start0, d.start1);
+            c.ref_h = d.heuristic == 1;
+            c.ref_moves = d.moves == 1;
+        }
+        __syncthreads();
+    }
+
+    static __device__ __forceinline__ Tab make_tab(const InstDesc& d) {
+        Tab t;
+        t.s = d.table;
+        t.mask = d.table_mask;
+        t.max_probe = d.max_probe;
+        return t;
+    }
+    static __device__ __forceinline__ uint64_t get(const Tab& t, KeyT k) {
+        if constexpr (KW == 1) return tab_get(t, k);
+        else return tab_get(t, uint64_t(k), uint64_t(k >> 64));
+    }
+    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old) {
+        if constexpr (KW == 1) return tab_insert(t, k, v, old);
+        else return tab_insert(t, uint64_t(k), uint64_t(k >> 64), v, old);
+    }
+    static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
+    static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
+    static __device__ __forceinline__ Pre prepare(const Ctx&, KeyT k) { return blank_of(k); }
+
+    static __device__ __forceinline__ bool succ(const Ctx& c, KeyT k, Pre p, int m, uint32_t pm,
+                                                uint32_t g, uint32_t h, KeyT& nk, uint32_t& ng,
+                                                uint32_t& nh) {
+        if ((uint32_t)(m ^ 1) == pm) return false;  // straight back to the parent
+        const int r = p / N, col = p % N;
+        int q;
+        if (m == 0) {
+            if (r >= N - 1) return false;
+            q = p + N;
+        } else if (m == 1) {
+            if (c.ref_moves || r == 0) return false;
+            q = p - N;
+        } else if (m == 2) {
+            if (col >= N - 1) return false;
+            q = p + 1;
+        } else {
+            if (c.ref_moves || col == 0) return false;
+            q = p - 1;
+        }
+        const uint32_t t = field(k, q);
+        nk = (k & ~(KeyT((1u << B) - 1) << (B * q))) | (KeyT(t) << (B * p));
+        nh = h + c.md[t][p] - c.md[t][q];
+        if (c.ref_h) nh = nh + c.md[0][q] - c.md[0][p];
+        ng = g + 1;
+        return true;
+    }
+
+    // Parent of k when k was reached with move m: the blank moves back.
+    static __device__ __forceinline__ KeyT parent(const Ctx&, KeyT k, uint32_t m) {
+        const int p = blank_of(k);
+        const int q = (m == 0) ? p - N : (m == 1) ? p + N : (m == 2) ? p - 1 : p + 1;
+        const uint32_t t = field(k, q);
+        return (k & ~(KeyT((1u << B) - 1) << (B * q))) | (KeyT(t) << (B * p));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Weighted grid, 8-connected (a_star_pathfinding.h:147-209).  Key = cell index
+// y*W + x.  Move m shifts (x, y) by (DX[m], DY[m]); entering a cell costs its
+// weight; weight 0 is impassable.  The duplicate-detection table is a dense
+// value array indexed by cell.
+// ---------------------------------------------------------------------------
+struct GridDom {
+    static constexpr int KW = 1;
+    static constexpr int MAXN = 8;
+    using KeyT = uint64_t;
+    using Tab = DenseTab;
+    struct Pre { int x, y; };
+
+    struct Ctx {
+        const uint8_t* w;
+        uint32_t W, H, goal, start, gx, gy, minw, href;
+    };
+
+    static __device__ __forceinline__ int dx(int m) { return (m == 0 || m == 4 || m == 5) ? 1 : (m == 1 || m == 6 || m == 7) ? -1 : 0; }
+    static __device__ __forceinline__ int dy(int m) { return (m == 2 || m == 4 || m == 6) ? 1 : (m == 3 || m == 5 || m == 7) ? -1 : 0; }
+    static __device__ __forceinline__ uint32_t inv(uint32_t m) { return m < 4 ? (m ^ 1) : 11 - m; }
+
+    static __device__ __forceinline__ KeyT key_of(const Entry<1>& e) { return e.k0; }
+    static __device__ __forceinline__ void set_key(Entry<1>& e, KeyT k) { e.k0 = k; }
+
+    static __device__ void load(Ctx& c, const InstDesc& d) {
+        if (threadIdx.x == 0) {
+            c.w = d.weights;
+            c.W = d.W;
+            c.H = d.H;
+            c.goal = (uint32_t)d.goal0;
+            c.start = (uint32_t)d.start0;
+            c.gx = c.goal % d.W;
+            c.gy = c.goal / d.W;
+            c.minw = d.minw;
+            c.href = d.heuristic;
+        }
+        __syncthreads();
+    }
+    static __device__ __forceinline__ Tab make_tab(const InstDesc& d) { return Tab{d.table}; }
+    static __device__ __forceinline__ uint64_t get(const Tab& t, KeyT k) { return __ldcg(t.v + k); }
+    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old) {
+        old = atomicMin(t.v + k, v);
+        return old == kEmpty ? 1 : 0;
+    }
+    static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
+    static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
+    static __device__ __forceinline__ Pre prepare(const Ctx& c, KeyT k) {
+        const uint32_t cell = (uint32_t)k;
+        return Pre{(int)(cell % c.W), (int)(cell / c.W)};
+    }
+    static __device__ __forceinline__ uint32_t heur(const Ctx& c, int x, int y) {
+        // 0: Chebyshev x min weight (admissible); 1: Manhattan (the reference's,
+        // a_star_pathfinding.h:219-221); 2: zero.
+        const uint32_t ax = (uint32_t)abs(x - (int)c.gx), ay = (uint32_t)abs(y - (int)c.gy);
+        if (c.href == 1) return ax + ay;
+        if (c.href == 2) return 0;
+        return (ax > ay ? ax : ay) * c.minw;
+    }
+    static __device__ __forceinline__ bool succ(const Ctx& c, KeyT, Pre p, int m, uint32_t pm,
+                                                uint32_t g, uint32_t, KeyT& nk, uint32_t& ng,
+                                                uint32_t& nh) {
+        if (pm != kRootMove && (uint32_t)m == inv(pm)) return false;
+        const int nx = p.x + dx(m), ny = p.y + dy(m);
+        if (nx < 0 || ny < 0 || nx >= (int)c.W || ny >= (int)c.H) return false;
+        const uint32_t cell = (uint32_t)ny * c.W + (uint32_t)nx;
+        const uint32_t wt = __ldg(c.w + cell);
+        if (!wt) return false;
+        nk = cell;
+        ng = g + wt;
+        nh = heur(c, nx, ny);
+        return true;
+    }
+    static __device__ __forceinline__ KeyT parent(const Ctx& c, KeyT k, uint32_t m) {
+        return (KeyT)((int64_t)k - dx((int)m) - (int64_t)dy((int)m) * (int64_t)c.W);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Block-shared state.
+// ---------------------------------------------------------------------------
+struct CtaShared {
+    TeamSlot slot[3];  // team slots of a one-block team
+    InstDesc desc;
+    uint32_t inst, run_best, ok, pad;
+    union {
+        SlidingDom<3>::Ctx s3;
+        SlidingDom<4>::Ctx s4;
+        SlidingDom<5>::Ctx s5;
+        GridDom::Ctx g;
+    } ctx;
+};
+
+extern __shared__ uint4 g_dyn_smem[];
+
+// Barrier over the blocks of a multi-block team: sense via a generation
+// counter, bounded wait (deadline on the device clock), abort flag so that
+// one block giving up releases the others.
+__device__ __forceinline__ bool team_sync_grid(TeamCtl* tc, uint32_t nctas, uint64_t timeout_ns,
+                                               CtaShared& sm) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ok = 1;
+        volatile uint32_t* vgen = &tc->gen;
+        volatile uint32_t* vab = &tc->abort;
+        const uint32_t g = *vgen;
+        __threadfence();
+        if (atomicAdd(&tc->arrive, 1u) == nctas - 1) {
+            atomicExch(&tc->arrive, 0u);
+            __threadfence();
+            atomicAdd(&tc->gen, 1u);
+        } else {
+            const uint64_t t0 = globaltimer_ns();
+            for (uint32_t spin = 1;; ++spin) {
+                if (*vgen != g) break;
+                if (*vab) { ok = 0; break; }
+                if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+                    atomicExch(&tc->abort, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        if (*vab) ok = 0;
+        sm.ok = ok;
+    }
+    __syncthreads();
+    return sm.ok != 0;
+}
+
+__device__ __forceinline__ uint32_t ld_vol(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+__device__ __forceinline__ uint64_t ld_vol64(const unsigned long long* p) {
+    return *(const volatile unsigned long long*)p;
+}
+
+template <class D>
+__device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared& sm,
+                             typename D::Ctx& ctx) {
+    constexpr int KW = D::KW;
+    using E = Entry<KW>;
+    using KeyT = typename D::KeyT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const bool multi = P.team_ctas > 1;
+    const uint32_t rank = multi ? blockIdx.x : 0;
+    const uint32_t H = d.heaps;
+    TeamSlot* slots = multi ? P.team->slot : sm.slot;
+    E* stage = multi ? reinterpret_cast<E*>(P.stage) : reinterpret_cast<E*>(g_dyn_smem);
+    InstCtl* ctl = d.ctl;
+    const bool leader = rank == 0 && threadIdx.x == 0;
+
+    auto tsync = [&]() -> bool {
+        if (!multi) {
+            __syncthreads();
+            return true;
+        }
+        return team_sync_grid(P.team, P.team_ctas, P.barrier_timeout_ns, sm);
+    };
+
+    D::load(ctx, d);
+    const typename D::Tab tab = D::make_tab(d);
+
+    WarpHeap<KW> hp;
+    const uint32_t hid = rank * W + warp;
+    hp.nodes = reinterpret_cast<E*>(d.heap_nodes) + (size_t)hid * (d.heap_cap + 1) * 32;
+    hp.hdr = d.heap_hdr + 2 * hid;
+    hp.cap = d.heap_cap;
+
+    const uint32_t life = ld_vol(&ctl->life);
+    if (!multi && threadIdx.x < 3) {
+        sm.slot[threadIdx.x].minprio = kInfPrio;
+        sm.slot[threadIdx.x].count = 0;
+        sm.slot[threadIdx.x].best = kInf;
+        sm.slot[threadIdx.x].err = 0;
+    }
+    uint32_t status = kInf;  // kInf while running / suspended
+    if (life == LIFE_FRESH) {
+        // Clear the table (0xff = empty key and value) across the whole team.
+        uint4* tp = reinterpret_cast<uint4*>(d.table);
+        const uint64_t n16 = d.table_words / 2;
+        const uint64_t stride = (uint64_t)P.team_ctas * blockDim.x;
+        for (uint64_t i = (uint64_t)rank * blockDim.x + threadIdx.x; i < n16; i += stride)
+            __stcg(tp + i, make_uint4(~0u, ~0u, ~0u, ~0u));
+        if ((d.table_words & 1) && rank == 0 && threadIdx.x == 0)  // odd cell count: last word
+            __stcg(d.table + d.table_words - 1, kEmpty);
+        heap_init(hp);
+        if (!tsync()) status = ST_BARRIER;
+        if (hid == 0) {
+            E s = inf_entry<KW>();
+            s.prio = make_prio(d.f0, 0);
+            D::set_key(s, ctx.start);
+            if (lane == 0) hp.part = s;
+            hp.pc = 1;
+        }
+        if (leader) {
+            uint64_t old;
+            D::insert(tab, ctx.start, make_val(0, kRootMove), old);
+            atomicAdd(&ctl->table_used, 1ull);
+            ctl->t_start = globaltimer_ns();
+        }
+        if (threadIdx.x == 0) sm.run_best = D::is_goal(ctx, ctx.start) ? 0u : kInf;
+    } else {
+        heap_restore(hp, lane);
+        if (threadIdx.x == 0) sm.run_best = ld_vol(&ctl->best);
+    }
+    if (status == kInf && !tsync()) status = ST_BARRIER;
+
+    const uint32_t ew = d.ew;
+    uint32_t it = 0;
+    const uint32_t it0 = ld_vol(&ctl->iterations);
+    while (status == kInf) {
+        const uint32_t s = it % 3;
+        TeamSlot* S = slots + s;
+        const uint32_t rb = sm.run_best;
+
+        // ---- pop + expand + insert-or-min ----
+        E e;
+        const uint32_t cnt = heap_pop(hp, ew, e, lane);
+        bool act = (uint32_t)lane < cnt;
+        const KeyT k = D::key_of(e);
+        const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
+        uint32_t pm = kRootMove;
+        bool stale = false;
+        if (act) {
+            const uint64_t v = D::get(tab, k);
+            if ((uint32_t)(v >> 32) < g) {
+                stale = true;
+                act = false;
+            } else {
+                pm = (uint32_t)v & 0xffu;
+            }
+        }
+        if (act && D::is_goal(ctx, k)) {
+            atomicMin(&S->best, g);
+            act = false;
+        }
+        const unsigned bexp = __ballot_sync(kFull, act), bstale = __ballot_sync(kFull, stale);
+        const typename D::Pre pre = D::prepare(ctx, k);
+        uint32_t n_gen = 0, n_claim = 0, n_push = 0;
+        bool tfull = false;
+#pragma unroll
+        for (int m = 0; m < D::MAXN; ++m) {
+            E out = inf_entry<KW>();
+            bool acc = false;
+            if (act) {
+                KeyT nk;
+                uint32_t ng, nh;
+                if (D::succ(ctx, k, pre, m, pm, g, h, nk, ng, nh)) {
+                    ++n_gen;
+                    const uint32_t nf = ng + nh;
+                    if (nf < rb) {
+                        uint64_t old;
+                        const int r = D::insert(tab, nk, make_val(ng, (uint32_t)m), old);
+                        if (r < 0) {
+                            tfull = true;
+                        } else {
+                            n_claim += (uint32_t)r;
+                            if ((uint32_t)(old >> 32) > ng) {
+                                acc = true;
+                                out.prio = make_prio(nf, ng);
+                                D::set_key(out, nk);
+                                if (D::is_goal(ctx, nk)) atomicMin(&S->best, ng);
+                            }
+                        }
+                    }
+                }
+            }
+            const unsigned bal = __ballot_sync(kFull, acc);
+            if (bal) {
+                const int ldr = __ffs(bal) - 1;
+                uint32_t base = 0;
+                if (lane == ldr) base = atomicAdd(&S->count, (uint32_t)__popc(bal));
+                base = __shfl_sync(kFull, base, ldr);
+                if (acc) st_stage(stage + base + __popc(bal & ((1u << lane) - 1u)), out, multi);
+                n_push += (uint32_t)__popc(bal);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            n_gen += __shfl_xor_sync(kFull, n_gen, o);
+            n_claim += __shfl_xor_sync(kFull, n_claim, o);
+        }
+        const bool any_full = __any_sync(kFull, tfull);
+        if (lane == 0) {
+            if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
+            if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
+            if (n_gen) atomicAdd(&ctl->generated, (unsigned long long)n_gen);
+            if (n_push) atomicAdd(&ctl->pushes, (unsigned long long)n_push);
+            if (n_claim) atomicAdd(&ctl->table_used, (unsigned long long)n_claim);
+            if (any_full) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+        }
+        if (!tsync()) {
+            status = ST_BARRIER;
+            break;
+        }
+
+        // ---- push: deal stage chunks to the warp-heaps ----
+        const uint32_t total = ld_vol(&S->count);
+        const uint32_t nch = (total + 31) / 32;
+        bool hfull = false;
+        for (uint32_t c = (hid + H - it % H) % H; c < nch; c += H) {
+            const uint32_t idx = c * 32 + (uint32_t)lane;
+            E x = idx < total ? ld_stage(stage + idx, multi) : inf_entry<KW>();
+            const uint32_t m = total - c * 32 < 32 ? total - c * 32 : 32;
+            if (!heap_push(hp, x, m, lane)) {
+                hfull = true;
+                break;
+            }
+        }
+        const uint64_t mp = heap_min(hp);
+        if (lane == 0) {
+            atomicMin(&S->minprio, (unsigned long long)mp);
+            if (hfull) atomicCAS(&S->err, 0u, (uint32_t)ST_HEAP_FULL);
+        }
+        if (threadIdx.x == 0) {
+            const uint32_t sb = ld_vol(&S->best);
+            if (sb < sm.run_best) sm.run_best = sb;
+        }
+        if (leader) {
+            TeamSlot* nx = slots + (s + 1) % 3;
+            nx->minprio = kInfPrio;
+            nx->count = 0;
+            nx->best = kInf;
+            nx->err = 0;
+            if (d.max_exp && ld_vol64(&ctl->expansions) >= d.max_exp) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
+            if (d.max_iter && it0 + it + 1 >= d.max_iter) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
+            if (d.timeout_ns && globaltimer_ns() - ctl->t_start > d.timeout_ns)
+                atomicCAS(&S->err, 0u, (uint32_t)ST_TIMEOUT);
+        }
+        if (!tsync()) {
+            status = ST_BARRIER;
+            break;
+        }
+        const uint32_t err = ld_vol(&S->err);
+        const uint64_t gm = ld_vol64(&S->minprio);
+        const uint32_t best = sm.run_best;
+        ++it;
+        // Termination (a_star.h:260-262): best goal cost <= min f of the open list.
+        // An iteration that lost entries (full table or heap) cannot prove optimality.
+        const bool found = best != kInf && best <= prio_f(gm);
+        if (err == ST_TABLE_FULL || err == ST_HEAP_FULL) status = err;
+        else if (found) status = ST_OK;
+        else if (err) status = err;
+        else if (gm == kInfPrio) status = ST_NO_PATH;
+        else if (P.slice_iters && it >= P.slice_iters) break;  // suspend
+    }
+
+    if (lane == 0) atomicMax(&ctl->max_nodes, hp.max_n);
+    if (status == kInf) {  // suspended: keep the search state resident
+        heap_save(hp, lane);
+        if (leader) {
+            ctl->best = sm.run_best;
+            ctl->iterations = it0 + it;
+            __threadfence();
+            ctl->life = LIFE_RUNNING;
+        }
+        return;
+    }
+    if (leader) {
+        ctl->best = sm.run_best;
+        ctl->iterations = it0 + it;
+        ctl->status = status;
+        __threadfence();
+        ctl->life = LIFE_DONE;
+    }
+}
+
+template <uint32_t KINDS>
+__device__ __forceinline__ void dispatch(const LaunchParams& P, CtaShared& sm) {
+    switch (sm.desc.kind) {
+        case KIND_SLIDING3:
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING3)) != 0) run_instance<SlidingDom<3>>(P, sm.desc, sm, sm.ctx.s3);
+            break;
+        case KIND_SLIDING4:
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING4)) != 0) run_instance<SlidingDom<4>>(P, sm.desc, sm, sm.ctx.s4);
+            break;
+        case KIND_SLIDING5:
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING5)) != 0) run_instance<SlidingDom<5>>(P, sm.desc, sm, sm.ctx.s5);
+            break;
+        case KIND_GRID:
+            if constexpr ((KINDS & kind_bit(KIND_GRID)) != 0) run_instance<GridDom>(P, sm.desc, sm, sm.ctx.g);
+            break;
+        default:
+            break;
+    }
+}
+
+// Persistent search kernel.  One-block teams take instances from a work
+// counter until none is left; a multi-block team (cooperative launch) runs
+// instance 0 on every block.
+template <uint32_t KINDS>
+__global__ void __launch_bounds__(512, 1) search_kernel(LaunchParams P) {
+    __shared__ CtaShared sm;
+    if (P.team_ctas > 1) {
+        if (threadIdx.x == 0) sm.desc = P.insts[0];
+        __syncthreads();
+        dispatch<KINDS>(P, sm);
+        return;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) sm.inst = atomicAdd(P.next, 1u);
+        __syncthreads();
+        const uint32_t i = sm.inst;
+        if (i >= P.n_insts) break;
+        if (threadIdx.x == 0) sm.desc = P.insts[P.order ? P.order[i] : i];
+        __syncthreads();
+        dispatch<KINDS>(P, sm);
+        __syncthreads();
+    }
+}
+
+// Path rebuild (a_star.h:268-281 walked one <<<1,1>>> launch per step): one
+// thread per finished instance follows parent moves from the goal to the
+// start twice -- once to count, once to write the states goal-first into a
+// slice of the shared path arena reserved with one atomic.
+template <class D>
+__device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long long* arena,
+                          unsigned long long arena_words, unsigned long long* arena_used) {
+    InstCtl* ctl = d.ctl;
+    const typename D::Tab tab = D::make_tab(d);
+    // Every step lowers g by at least 1, so a walk longer than best + 1 states
+    // means a damaged table.
+    const uint64_t limit = (uint64_t)ctl->best + 2;
+    uint64_t len = 1;
+    for (typename D::KeyT k = ctx.goal; !D::is_start(ctx, k); ++len) {
+        const uint64_t v = D::get(tab, k);
+        const uint32_t m = (uint32_t)v & 0xffu;
+        if (v == kEmpty || m == kRootMove || len > limit) {
+            ctl->status = ST_PATH_CAP;
+            ctl->path_len = 0;
+            return;
+        }
+        k = D::parent(ctx, k, m);
+    }
+    const unsigned long long words = len * D::KW;
+    const unsigned long long off = atomicAdd(arena_used, words);
+    ctl->path_len = (uint32_t)len;
+    if (off + words > arena_words) {
+        ctl->status = ST_PATH_CAP;
+        return;
+    }
+    ctl->path_off = off;
+    typename D::KeyT k = ctx.goal;
+    for (uint64_t i = 0; i < len; ++i) {
+        unsigned long long* o = arena + off + i * D::KW;
+        o[0] = (uint64_t)k;
+        if constexpr (D::KW == 2) o[1] = (uint64_t)(k >> 64);
+        if (i + 1 < len) k = D::parent(ctx, k, (uint32_t)D::get(tab, k) & 0xffu);
+    }
+}
+
+// Builds the domain context without the block-wide table fill (one thread).
+template <int N> __device__ void sliding_ctx_min(typename SlidingDom<N>::Ctx& c, const InstDesc& d) {
+    c.goal = SlidingDom<N>::desc_key(d.goal0, d.goal1);
+    c.start = SlidingDom<N>::desc_key(d.start0, d.start1);
+}
+
+static __global__ void path_kernel(const InstDesc* insts, uint32_t n, unsigned long long* arena,
+                            unsigned long long arena_words, unsigned long long* arena_used) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const InstDesc& d = insts[i];
+    if (d.ctl->life != LIFE_DONE || d.ctl->status != ST_OK) return;
+    switch (d.kind) {
+        case KIND_SLIDING3: {
+            SlidingDom<3>::Ctx c;
+            sliding_ctx_min<3>(c, d);
+            walk_path<SlidingDom<3>>(d, c, arena, arena_words, arena_used);
+            break;
+        }
+        case KIND_SLIDING4: {
+            SlidingDom<4>::Ctx c;
+            sliding_ctx_min<4>(c, d);
+            walk_path<SlidingDom<4>>(d, c, arena, arena_words, arena_used);
+            break;
+        }
+        case KIND_SLIDING5: {
+            SlidingDom<5>::Ctx c;
+            sliding_ctx_min<5>(c, d);
+            walk_path<SlidingDom<5>>(d, c, arena, arena_words, arena_used);
+            break;
+        }
+        case KIND_GRID: {
+            GridDom::Ctx c;
+            c.W = d.W;
+            c.goal = (uint32_t)d.goal0;
+            c.start = (uint32_t)d.start0;
+            walk_path<GridDom>(d, c, arena, arena_words, arena_used);
+            break;
+        }
+        default:
+            break;
+    }
+}
+
+}  // namespace gastar

@@ -1,0 +1,186 @@
+/*
+ * gastar — GA* (massively parallel A*) search engine for one NVIDIA GB300.
+ * C ABI of libgastar.so.  Plain pointers and sizes only; every function
+ * returns a status code instead of throwing.
+ *
+ * Each entry point names the reference interface (michalborkowski96/cuda_a_star)
+ * it replaces.  Boards are n*n bytes row-major with 0 for the blank (the
+ * reference's SlidingPuzzle::Position<size>::board, a_star_sliding_puzzle.h:14-18);
+ * grids are w*h bytes indexed y*w + x holding the cost of entering the cell,
+ * 0 for an impassable cell (the reference's obstacle and cost lists,
+ * a_star_pathfinding.h:74-81, in dense form).
+ */
+#ifndef GASTAR_H
+#define GASTAR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (per call and per solve) ---- */
+enum gastar_status {
+    GASTAR_OK = 0,             /* call succeeded / path found */
+    GASTAR_NO_PATH = 1,        /* search space exhausted without reaching the goal */
+    GASTAR_BUDGET = 2,         /* expansion or iteration budget exhausted */
+    GASTAR_TIMEOUT = 3,        /* wall-clock deadline reached on the device */
+    GASTAR_HEAP_FULL = 4,      /* a priority-queue partition ran out of nodes */
+    GASTAR_TABLE_FULL = 5,     /* the duplicate-detection table passed its load limit */
+    GASTAR_PATH_CAP = 6,       /* caller's path buffer too small (path_len holds the need) */
+    GASTAR_BARRIER_TIMEOUT = 7,/* a device-side wait gave up (bounded spin) */
+    GASTAR_BAD_INPUT = 8,      /* malformed instance or argument */
+    GASTAR_CUDA_ERROR = 9,     /* CUDA runtime error (see gastar_last_error) */
+    GASTAR_NO_DEVICE = 10,     /* no usable GPU */
+    GASTAR_PENDING = 11,       /* serving: request not finished yet */
+    GASTAR_OUT_OF_MEMORY = 12, /* device memory budget exceeded */
+};
+
+enum gastar_heuristic {
+    GASTAR_H_ADMISSIBLE = 0, /* tile Manhattan without the blank; Chebyshev x min weight on grids */
+    GASTAR_H_REFERENCE = 1,  /* the reference's formulas: Manhattan incl. blank
+                                (a_star_sliding_puzzle.h:152-163); Manhattan on grids
+                                (a_star_pathfinding.h:219-221).  Not admissible. */
+    GASTAR_H_ZERO = 2,       /* h = 0 (Dijkstra order) */
+};
+
+enum gastar_moves {
+    GASTAR_MOVES_STANDARD = 0,  /* blank moves to any of its 4 neighbours */
+    GASTAR_MOVES_REFERENCE = 1, /* the reference's successor arithmetic: only moves 0 (row+1)
+                                   and 2 (col+1) exist (a_star_sliding_puzzle.h:106-111) */
+};
+
+/* Search parameters.  Zero fields take defaults (gastar_config_default). */
+typedef struct gastar_config {
+    uint32_t num_queues;       /* parallel pops per iteration (reference Q, main.cu:18) */
+    uint32_t heuristic;        /* gastar_heuristic */
+    uint32_t moves;            /* gastar_moves (sliding puzzles only) */
+    uint32_t expansion_width;  /* entries each warp-heap pops per iteration, 1..32 */
+    uint32_t warps_per_block;  /* warp-heaps per thread block, 1..16 */
+    uint32_t max_blocks;       /* cap on thread blocks for one instance (0 = all SMs) */
+    float load_factor;         /* table load limit before GASTAR_TABLE_FULL (0.5..0.9) */
+    uint32_t table_log2;       /* hash-table slots = 2^table_log2 (0 = adaptive) */
+    uint64_t heap_entries;     /* priority-queue capacity per instance (0 = adaptive) */
+    uint64_t max_expansions;   /* 0 = unlimited */
+    uint32_t max_iterations;   /* 0 = unlimited */
+    uint32_t timeout_ms;       /* device-side deadline, 0 = none */
+    uint32_t regrow;           /* plain engine: re-run with doubled capacity on *_FULL (default 1) */
+    uint32_t reserved;
+    void *stream;              /* cudaStream_t to launch on (NULL = the context's stream) */
+} gastar_config;
+
+/* Outcome of one solve. */
+typedef struct gastar_result {
+    int32_t status;            /* gastar_status */
+    uint32_t cost;             /* path cost (valid when status == GASTAR_OK) */
+    uint32_t path_len;         /* states on the path, start and goal included */
+    uint32_t iterations;       /* GA* iterations (pop/expand/push rounds) */
+    uint64_t expansions;       /* non-stale pops that generated successors */
+    uint64_t generated;        /* successors produced by the move function */
+    uint64_t pushes;           /* successors that improved the table and were queued */
+    uint64_t stale;            /* pops discarded because the table held a lower g */
+    uint64_t table_used;       /* states stored in the duplicate-detection table */
+    float kernel_ms;           /* device time of the search kernel(s), CUDA events */
+    float total_ms;            /* host wall time of the call */
+    uint32_t attempts;         /* plain engine: solves run (1 + regrows) */
+    uint32_t reserved;
+} gastar_result;
+
+typedef struct gastar_ctx gastar_ctx;
+
+/* ---- context ---- */
+void gastar_config_default(gastar_config *cfg);
+/* Creates a context on `device` (-1 = current).  Returns NULL on failure. */
+gastar_ctx *gastar_create(int device);
+void gastar_destroy(gastar_ctx *ctx);
+const char *gastar_last_error(void);
+const char *gastar_status_name(int status);
+int gastar_version(void);
+/* Device properties the engine sized itself with: SM count, device memory. */
+int gastar_device_info(gastar_ctx *ctx, int *sm_count, uint64_t *mem_bytes, char *name,
+                       size_t name_len);
+
+/* ---- plain GA*: one instance per launch ----
+ * Replaces SlidingPuzzle::solve<size> + a_star<Position<size>, 4, ...>
+ * (a_star_sliding_puzzle.h:165-171, a_star.h:223-282).  `path` receives up to
+ * path_cap boards (n*n bytes each), start first.  path may be NULL. */
+int gastar_solve_sliding(gastar_ctx *ctx, uint32_t n, const uint8_t *start, const uint8_t *goal,
+                         const gastar_config *cfg, uint8_t *path, uint32_t path_cap,
+                         gastar_result *out);
+/* Replaces Pathfinding::solve + a_star<Position, 8, ...> (a_star_pathfinding.h:223-238).
+ * `path` receives cell indices (y*w + x), start first. */
+int gastar_solve_grid(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint8_t *weights,
+                      uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty,
+                      const gastar_config *cfg, uint32_t *path, uint32_t path_cap,
+                      gastar_result *out);
+/* Device-resident variant of gastar_solve_grid: `d_weights` is a device
+ * pointer; nothing is copied host->device.  path may be NULL. */
+int gastar_solve_grid_device(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint8_t *d_weights,
+                             uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty,
+                             const gastar_config *cfg, uint32_t *path, uint32_t path_cap,
+                             gastar_result *out);
+
+/* ---- batched GA*: many instances in one persistent launch ----
+ * No reference counterpart (the reference solves one instance per process,
+ * its problem data lives in __constant__ symbols: a_star_sliding_puzzle.h:125-128,
+ * a_star_pathfinding.h:72-81). */
+typedef struct gastar_batch gastar_batch;
+typedef struct gastar_batch_config {
+    uint32_t warps_per_block;  /* warp-heaps per instance (queue count) */
+    uint32_t expansion_width;  /* pops per warp-heap per iteration */
+    float load_factor;         /* hash-table load factor used to size partitions */
+    uint32_t heuristic, moves;
+    uint32_t use_graph;        /* capture the launch sequence in a CUDA graph */
+    uint32_t blocks;           /* persistent blocks (0 = occupancy x SMs) */
+    uint32_t timeout_ms;
+    uint64_t max_expansions;   /* per instance */
+    uint64_t sliding_states;   /* expected max states per puzzle instance (0 = by size) */
+} gastar_batch_config;
+
+void gastar_batch_config_default(gastar_batch_config *cfg);
+gastar_batch *gastar_batch_create(gastar_ctx *ctx, const gastar_batch_config *cfg);
+void gastar_batch_destroy(gastar_batch *b);
+/* Returns the instance index (>= 0) or a negative gastar_status. */
+int gastar_batch_add_sliding(gastar_batch *b, uint32_t n, const uint8_t *start,
+                             const uint8_t *goal);
+int gastar_batch_add_grid(gastar_batch *b, uint32_t w, uint32_t h, const uint8_t *weights,
+                          uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty);
+/* Allocates partitions, uploads instances (host->device) and solves them all. */
+int gastar_batch_run(gastar_batch *b);
+/* Re-solves the already uploaded instances (inputs resident in device memory). */
+int gastar_batch_rerun(gastar_batch *b);
+uint32_t gastar_batch_count(const gastar_batch *b);
+int gastar_batch_result(gastar_batch *b, uint32_t index, gastar_result *out);
+/* Copies the path of one solved instance: boards (sliding) or cell indices (grid). */
+int gastar_batch_path(gastar_batch *b, uint32_t index, void *path, uint32_t path_cap,
+                      uint32_t *path_len);
+/* Device time of the last run's kernel(s) and the bytes copied each way. */
+int gastar_batch_stats(gastar_batch *b, float *kernel_ms, uint64_t *h2d_bytes,
+                       uint64_t *d2h_bytes, uint64_t *device_bytes);
+
+/* ---- text formats and synthetic instances (host only, no GPU needed) ---- */
+/* Reads "start goal" in the reference's sliding format (Position(std::istream&),
+ * a_star_sliding_puzzle.h:21-48): n*n comma-separated ints, "_" or "0" = blank. */
+int gastar_parse_sliding(const char *text, uint32_t n, uint8_t *start, uint8_t *goal);
+/* Prints a board like the reference's operator<< (a_star_sliding_puzzle.h:59-74). */
+int gastar_format_sliding(uint32_t n, const uint8_t *board, char *out, size_t cap);
+/* Reads the grid header "W,H" (a_star_pathfinding.h:224). */
+int gastar_parse_grid_dims(const char *text, uint32_t *w, uint32_t *h);
+/* Reads the full grid document (a_star_pathfinding.h:223-231, 83-128) into a
+ * dense w*h weight array: unlisted cells cost 1, obstacles 0. */
+int gastar_parse_grid(const char *text, uint32_t w, uint32_t h, uint8_t *weights, uint32_t *sx,
+                      uint32_t *sy, uint32_t *tx, uint32_t *ty);
+/* Seeded instances: goal 0..n*n-1 row-major, start = non-reversing random
+ * walk of uniform length in [walk_min, walk_max] (SplitMix64 stream). */
+int gastar_gen_sliding(uint32_t n, uint64_t seed, uint32_t walk_min, uint32_t walk_max,
+                       uint8_t *start, uint8_t *goal);
+/* Seeded grid: weights uniform in [wmin, wmax], Bernoulli(density) obstacles,
+ * random monotone corridor (0,0) -> (w-1,h-1) kept passable. */
+int gastar_gen_grid(uint32_t w, uint32_t h, uint64_t seed, double density, uint32_t wmin,
+                    uint32_t wmax, uint8_t *weights);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

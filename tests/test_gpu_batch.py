@@ -1,0 +1,59 @@
+"""Batched GA* (one persistent launch) against the oracle and the plain engine."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_batch_matches_oracle(engine, oracle, gastar):
+    b = engine.batch(warps_per_block=8, expansion_width=32)
+    cases = []
+    for i in range(24):
+        s, g = gastar.gen_sliding(4, 500 + i, 20, 50)
+        cases.append(("s4", s, g, b.add_sliding(s, g)))
+    for i in range(8):
+        s, g = gastar.gen_sliding(3, 600 + i, 60, 60)
+        cases.append(("s3", s, g, b.add_sliding(s, g)))
+    for i in range(3):
+        s, g = gastar.gen_sliding(5, 700 + i, 10, 20)
+        cases.append(("s5", s, g, b.add_sliding(s, g)))
+    for i in range(12):
+        side = 40 + 23 * i
+        wts = gastar.gen_grid(side, side + 7, 800 + i, 0.2)
+        cases.append(("grid", wts, ((0, 0), (side - 1, side + 6)), b.add_grid(wts, (0, 0), (side - 1, side + 6))))
+    bad = np.arange(16, dtype=np.uint8)
+    bad[[1, 2]] = bad[[2, 1]]
+    cases.append(("bad", bad, np.arange(16, dtype=np.uint8), b.add_sliding(bad, np.arange(16, dtype=np.uint8))))
+    b.run()
+    for kind, a, c, idx in cases:
+        r = b.result(idx)
+        if kind == "bad":
+            assert r.status_name == "NO_PATH"
+            continue
+        if kind == "grid":
+            st, gl = c
+            o, _ = oracle.grid_astar(a, st, gl, path=False)
+            assert r.status_name == "OK" and r.cost == o.cost, (idx, r.status_name)
+            assert oracle.grid_validate(a, st, gl, r.path) == (True, r.cost)
+        else:
+            n = {"s3": 3, "s4": 4, "s5": 5}[kind]
+            o, _ = oracle.sliding_astar(n, a, c, path=False)
+            assert r.status_name == "OK" and r.cost == o.cost, (idx, kind, r.status_name, r.cost, o.cost)
+            assert oracle.sliding_validate(n, a, c, r.path) == (True, r.cost)
+    costs = [b.result(i, path=False).cost for _, _, _, i in cases]
+    b.rerun()   # inputs stay resident; graph replay
+    assert [b.result(i, path=False).cost for _, _, _, i in cases] == costs
+    st = b.stats()
+    assert st["kernel_ms"] > 0 and st["device_bytes"] > 0
+    b.close()
+
+
+def test_batch_equals_plain(engine, gastar):
+    b = engine.batch(warps_per_block=4, expansion_width=16)
+    inst = [gastar.gen_sliding(4, 900 + i, 30, 60) for i in range(8)]
+    for s, g in inst:
+        b.add_sliding(s, g)
+    b.run()
+    for i, (s, g) in enumerate(inst):
+        assert b.result(i, path=False).cost == engine.solve_sliding(s, g, 4, path=False).cost
+    b.close()
