@@ -1,0 +1,278 @@
+"""Benchmark of the GA* search path on one GB300.
+
+Default workload (the plain GA* configuration the metric is quoted on):
+64 15-puzzles, each scrambled from the goal by a seeded non-reversing random
+walk of uniform length 40-80, solved one instance per launch with 16384
+parallel pops per iteration and a 2^30-slot duplicate-detection table.  A
+step solves all 64 instances (search + path rebuild).
+
+Output: one JSON line (rank 0).  `value` = solves/s with the instances
+resident on the device (CUDA events on the launching stream); `e2e` = the same
+through the C ABI with host buffers, copies included; `cpu_baseline` = the
+single-thread host A* (the CPU oracle) over all host cores on the same
+instances.  `--impl reference` times that CPU implementation as the reference
+arm (the reference itself has no CPU path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "name": "P15 plain GA*: 64 x 15-puzzle (random walk 40-80 from goal 0..15), one instance "
+            "per launch, Q=16384 parallel pops, 2^30-slot table",
+    "n": 4, "instances": 64, "walk": (40, 80), "seed0": 0x15_0000, "num_queues": 16384,
+    "table_log2": 30,
+}
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def _instances(g):
+    n = WORKLOAD["n"]
+    lo, hi = WORKLOAD["walk"]
+    return [g.gen_sliding(n, WORKLOAD["seed0"] + i, lo, hi) for i in range(WORKLOAD["instances"])]
+
+
+def _oracle_run(insts, threads=0):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oracle_lib as o
+    starts = np.stack([s for s, _ in insts])
+    goals = np.stack([g for _, g in insts])
+    t0 = time.perf_counter()
+    used, res = o.sliding_batch(WORKLOAD["n"], starts, goals, heuristic=o.ADM, threads=threads)
+    dt = time.perf_counter() - t0
+    return used, res, dt
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.p = None
+        self.device = device
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_reference(args) -> dict:
+    """The CPU implementation of the path (host A*, all host threads)."""
+    import cuda_a_star_gb300 as g
+    insts = _instances(g)
+    for _ in range(args.warmup):
+        _oracle_run(insts)
+    times, used = [], 0
+    for _ in range(args.steps):
+        used, res, dt = _oracle_run(insts)
+        times.append(dt)
+    total = sum(times)
+    value = WORKLOAD["instances"] * args.steps / total
+    return {
+        "impl": "reference", "metric": "solves/s", "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "instances": WORKLOAD["instances"]},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port",
+                         "sample": f"all {WORKLOAD['instances']} instances per step, "
+                                   f"single-thread A* per instance over {used} host threads"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "expansions_per_s": sum(r.expansions for r in res) / times[-1],
+    }
+
+
+def run_ours(args) -> dict:
+    import numpy as np
+    import torch
+    import cuda_a_star_gb300 as g
+    from cuda_a_star_gb300 import build as engine_build
+
+    engine_build.build()
+    rank, world = _dist()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    eng = g.Engine(dev)
+    stream = torch.cuda.current_stream()
+    cfg = g.make_config(num_queues=WORKLOAD["num_queues"], table_log2=WORKLOAD["table_log2"],
+                        stream=stream.cuda_stream)
+    insts = _instances(g)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step(collect):
+        out = []
+        for s, goal in insts:
+            r = eng.solve_sliding(s, goal, WORKLOAD["n"], config=cfg, path=True, path_cap=1024)
+            if r.status != g.OK:
+                raise RuntimeError(f"solve failed: {r.status_name}")
+            if collect:
+                out.append(r)
+        return out
+
+    for _ in range(max(args.warmup, 0)):
+        step(False)
+    # --- device-timed steps (inputs resident; L2 flushed between steps) ---
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    step_ms, results = [], []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rs = step(True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        results.extend(rs)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    # --- end-to-end steps through the C ABI with host buffers ---
+    e2e_s, h2d, d2h = [], 0, 0
+    for k in range(args.steps):
+        flush.fill_((k + 7) & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = step(True)
+        torch.cuda.synchronize()
+        e2e_s.append(time.perf_counter() - t0)
+        h2d = sum(r.h2d_bytes for r in rs)
+        d2h = sum(r.d2h_bytes for r in rs)
+    ms = max(step_ms) if world == 1 else None
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_inst = WORKLOAD["instances"]
+    value = n_inst * args.steps * world / (total_ms / 1000.0)
+    exp = sum(r.expansions for r in results)
+    lat = sorted(r.total_ms for r in results)
+    kern_s = sum(r.kernel_ms for r in results) / 1000.0
+    alg_bytes = sum(16 * (r.expansions + r.stale) + 32 * r.generated + 48 * r.pushes for r in results)
+    launches = sum(r.launches for r in results)
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / kern_s / 1e9 if kern_s > 0 else 0.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "search_kernel_p15.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    out = {
+        "metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "instances": n_inst,
+                   "num_queues": WORKLOAD["num_queues"], "table_slots": 1 << WORKLOAD["table_log2"],
+                   "l2": "512 MiB buffer written between timed steps; 16 GiB table"},
+        "node_expansions_per_s": exp / (total_ms / 1000.0),
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(len(lat) * 0.99))]},
+        "e2e": {"value": n_inst * args.steps / sum(e2e_s), "unit": "solves/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "search_kernel",
+                     "algorithmic_bytes": "16 B per pop + 32 B per generated successor "
+                                          "+ 48 B per pushed successor"},
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        used, res, dt = _oracle_run(insts)
+        costs_gpu = [r.cost for r in results[:n_inst]]
+        agree = sum(1 for a, b in zip(costs_gpu, res) if a == b.cost) / n_inst
+        out["cpu_baseline"] = {"value": n_inst / dt, "unit": "solves/s", "cores": used,
+                               "kind": "port",
+                               "sample": f"the same {n_inst} instances once, single-thread host "
+                                         f"A* per instance over {used} threads"}
+        out["optimal_cost_agreement"] = agree
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    eng.close()
+    return out if rank == 0 else {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world = _dist()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        out = run_reference(args)
+    else:
+        out = run_ours(args)
+    if rank == 0 and out:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

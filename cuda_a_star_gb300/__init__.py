@@ -65,6 +65,9 @@ class SolveResult:
     kernel_ms: float = 0.0
     total_ms: float = 0.0
     attempts: int = 1
+    launches: int = 0
+    h2d_bytes: int = 0
+    d2h_bytes: int = 0
     extra: dict = field(default_factory=dict)
 
     @property
@@ -74,7 +77,8 @@ class SolveResult:
     @staticmethod
     def from_c(r: Result, path) -> "SolveResult":
         return SolveResult(r.status, r.cost, path, r.expansions, r.generated, r.pushes, r.stale,
-                           r.iterations, r.table_used, r.kernel_ms, r.total_ms, r.attempts)
+                           r.iterations, r.table_used, r.kernel_ms, r.total_ms, r.attempts,
+                           r.launches, r.h2d_bytes, r.d2h_bytes)
 
 
 def make_config(num_queues: int = 4096, heuristic: int = H_ADMISSIBLE,

@@ -33,7 +33,7 @@ class Config(C.Structure):
         ("max_blocks", C.c_uint32), ("load_factor", C.c_float), ("table_log2", C.c_uint32),
         ("heap_entries", C.c_uint64), ("max_expansions", C.c_uint64),
         ("max_iterations", C.c_uint32), ("timeout_ms", C.c_uint32), ("regrow", C.c_uint32),
-        ("reserved", C.c_uint32), ("stream", C.c_void_p),
+        ("delta", C.c_uint32), ("stream", C.c_void_p),
     ]
 
 
@@ -43,7 +43,7 @@ class Result(C.Structure):
         ("iterations", C.c_uint32), ("expansions", C.c_uint64), ("generated", C.c_uint64),
         ("pushes", C.c_uint64), ("stale", C.c_uint64), ("table_used", C.c_uint64),
         ("kernel_ms", C.c_float), ("total_ms", C.c_float), ("attempts", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("launches", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
     ]
 
 

@@ -288,11 +288,13 @@ template <int KW> __device__ void heap_sift_down(WarpHeap<KW>& h, int lane) {
     else st_entry(h.nodes + (size_t)idx * 32 + lane, cur);
 }
 
-// Pops the E (1..32) best entries; lane l < return value receives one.
+// Pops up to E (1..32) best entries whose priority is below `lim`; lane
+// l < return value receives one.  Nothing changes when no entry qualifies.
 template <int KW>
-__device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, Entry<KW>& out, int lane) {
+__device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, uint64_t lim, Entry<KW>& out, int lane) {
     if (h.N == 0) {
-        uint32_t c = E < h.pc ? E : h.pc;
+        const uint32_t below = __popc(__ballot_sync(kFull, (uint32_t)lane < h.pc && h.part.prio < lim));
+        const uint32_t c = E < below ? E : below;
         out = (uint32_t)lane < c ? h.part : inf_entry<KW>();
         Entry<KW> s = shfl_idx(h.part, (lane + (int)c) & 31);
         h.part = ((uint32_t)lane + c < h.pc) ? s : inf_entry<KW>();
@@ -301,6 +303,14 @@ __device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, Entry<KW>& out, int la
     }
     Entry<KW> lo, hi;
     merge2(h.root, h.part, lo, hi, lane);
+    {
+        const uint32_t below = __popc(__ballot_sync(kFull, lo.prio < lim));
+        if (below < E) E = below;
+        if (E == 0) {
+            out = inf_entry<KW>();
+            return 0;
+        }
+    }
     const uint32_t valid = 32 + h.pc, rest = valid - E;
     out = (uint32_t)lane < E ? lo : inf_entry<KW>();
     const int i1 = (int)E + lane, i2 = (int)E + 32 + lane;
@@ -407,9 +417,10 @@ struct HashTab64 {
     uint32_t max_probe;
 };
 
-// Returns 1 when the key was newly claimed, 0 when found, -1 when full.
+// Returns 1 when the key was newly claimed, 0 when found, -1 when full;
+// `slot` receives the slot's first word offset.
 __device__ __forceinline__ int tab_insert(const HashTab64& t, uint64_t key, uint64_t val,
-                                          uint64_t& old) {
+                                          uint64_t& old, uint64_t& slot) {
     uint64_t i = mix64(key) & t.mask;
     for (uint32_t p = 0; p < t.max_probe; ++p) {
         unsigned long long* ks = t.s + 2 * i;
@@ -424,6 +435,7 @@ __device__ __forceinline__ int tab_insert(const HashTab64& t, uint64_t key, uint
         }
         if (k == key) {
             old = atomicMin(ks + 1, val);
+            slot = 2 * i;
             return claimed;
         }
         i = (i + 1) & t.mask;
@@ -470,7 +482,7 @@ __device__ __forceinline__ uint64_t hash128(uint64_t k0, uint64_t k1) {
 }
 
 __device__ __forceinline__ int tab_insert(const HashTab128& t, uint64_t k0, uint64_t k1,
-                                          uint64_t val, uint64_t& old) {
+                                          uint64_t val, uint64_t& old, uint64_t& slot) {
     uint64_t i = hash128(k0, k1) & t.mask;
     for (uint32_t p = 0; p < t.max_probe; ++p) {
         unsigned long long* ks = t.s + 4 * i;
@@ -479,6 +491,7 @@ __device__ __forceinline__ int tab_insert(const HashTab128& t, uint64_t k0, uint
         int claimed = (o0 == kEmpty && o1 == kEmpty);
         if (claimed || (o0 == k0 && o1 == k1)) {
             old = atomicMin(ks + 2, val);
+            slot = 4 * i;
             return claimed;
         }
         i = (i + 1) & t.mask;

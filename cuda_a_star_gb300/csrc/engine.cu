@@ -44,8 +44,10 @@ void DevBuf::release() {
 }
 
 bool DevBuf::ensure(size_t bytes) {
+    fresh = false;
     if (bytes <= n) return true;
     release();
+    fresh = true;
     size_t want = bytes < 256 ? 256 : bytes;
     if (!cuda_ok(cudaMalloc(&p, want), "cudaMalloc")) {
         p = nullptr;
@@ -257,6 +259,8 @@ void gastar_destroy(gastar_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->table.release();
+    c->dense.release();
+    c->touched.release();
     c->heaps.release();
     c->hdr.release();
     c->stage.release();
@@ -307,10 +311,16 @@ static void fill_result(gastar_result* out, const InstCtl& c) {
     out->table_used = c.table_used;
 }
 
+struct AttemptStats {
+    float kernel_ms = 0;
+    uint32_t launches = 0;
+    uint64_t h2d = 0, d2h = 0;
+};
+
 // Runs the search (+ path rebuild) once with the given capacities.
 static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_config& cfg,
                          uint32_t table_log2, uint64_t heap_entries, bool want_path,
-                         cudaStream_t st, InstCtl& ctl_out, float& kernel_ms) {
+                         cudaStream_t st, InstCtl& ctl_out, AttemptStats& as) {
     const uint32_t kinds = kind_bit(pp.kind);
     const uint32_t ew = std::min(32u, std::max(1u, cfg.expansion_width ? cfg.expansion_width : 32u));
     const uint32_t W = std::min(16u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
@@ -330,30 +340,46 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         return GASTAR_CUDA_ERROR;
     }
     heaps = blocks * W;
+    const uint32_t maxn = max_neighbours(pp.kind);
 
-    // Table.
+    // Duplicate-detection table: a dense per-cell array for grids (cleared by
+    // the kernel), a hash table for puzzles that stays allocated across solves
+    // and is cleared slot by slot from the previous solve's claim list.
     const uint32_t ebytes = entry_bytes(pp.kind), kw = key_words(pp.kind);
-    uint64_t table_words, mask = 0, limit;
+    const uint32_t slot_words = kw == 1 ? 2 : 4;
+    uint64_t table_words, mask = 0, limit = ~0ull, touched_cap = 0;
+    DevBuf* tb;
     if (pp.kind == KIND_GRID) {
         table_words = (uint64_t)pp.W * pp.H;
-        limit = ~0ull;
+        tb = &c->dense;
+        if (!tb->ensure(table_words * 8)) return GASTAR_OUT_OF_MEMORY;
     } else {
         const uint64_t slots = 1ull << table_log2;
-        table_words = slots * (kw == 1 ? 2 : 4);
+        table_words = slots * slot_words;
         mask = slots - 1;
         float lf = cfg.load_factor > 0.f ? cfg.load_factor : 0.75f;
         lf = std::min(0.95f, std::max(0.1f, lf));
         limit = (uint64_t)((double)slots * lf);
+        touched_cap = limit + heaps * ew * maxn + 16;
+        tb = &c->table;
+        if (!tb->ensure(table_words * 8) || !c->touched.ensure(touched_cap * 4) || !c->misc.ensure(64))
+            return GASTAR_OUT_OF_MEMORY;
+        touched_cap = c->touched.n / 4;
+        if (tb->fresh || c->table_dirty) {
+            GA_CUDA(cudaMemsetAsync(tb->p, 0xff, tb->n, st));
+            GA_CUDA(cudaMemsetAsync(c->misc.p, 0, 8, st));  // claim-list length
+            c->table_dirty = false;
+        }
     }
     // Heaps: per warp-heap node capacity with headroom for uneven dealing.
     uint64_t per_heap = (heap_entries + heaps - 1) / heaps;
     uint64_t cap_nodes = std::max<uint64_t>(4, (per_heap * 2 + 31) / 32);
     if (cap_nodes > 0x7fffffffull) return GASTAR_OUT_OF_MEMORY;
     const size_t heap_bytes = (size_t)heaps * (cap_nodes + 1) * 32 * ebytes;
-    const size_t stage_entries = multi ? (size_t)heaps * ew * max_neighbours(pp.kind) : 0;
+    const size_t stage_entries = multi ? (size_t)heaps * ew * maxn : 0;
 
-    if (!c->table.ensure(table_words * 8) || !c->heaps.ensure(heap_bytes) ||
-        !c->hdr.ensure((size_t)heaps * 8) || !c->stage.ensure(std::max<size_t>(stage_entries * ebytes, 16)) ||
+    if (!c->heaps.ensure(heap_bytes) || !c->hdr.ensure((size_t)heaps * 8) ||
+        !c->stage.ensure(std::max<size_t>(stage_entries * ebytes, 16)) ||
         !c->desc.ensure(sizeof(InstDesc)) || !c->ctl.ensure(sizeof(InstCtl)) ||
         !c->team.ensure(sizeof(TeamCtl) + 64))
         return GASTAR_OUT_OF_MEMORY;
@@ -373,7 +399,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     d.H = pp.H;
     d.minw = pp.minw;
     d.f0 = pp.f0;
-    d.table = reinterpret_cast<unsigned long long*>(c->table.p);
+    d.table = reinterpret_cast<unsigned long long*>(tb->p);
     d.table_words = table_words;
     d.table_mask = mask;
     d.table_limit = limit;
@@ -386,7 +412,14 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     d.max_exp = cfg.max_expansions;
     d.timeout_ns = (uint64_t)cfg.timeout_ms * 1000000ull;
     d.max_iter = cfg.max_iterations;
+    d.delta = cfg.delta;
     d.ctl = reinterpret_cast<InstCtl*>(c->ctl.p);
+    if (pp.kind != KIND_GRID) {
+        d.touched = reinterpret_cast<uint32_t*>(c->touched.p);
+        d.touched_count = reinterpret_cast<unsigned long long*>(c->misc.p);
+        d.touched_cap = touched_cap;
+        d.prev_slot_words = c->prev_slot_words;
+    }
     c->h_desc = d;
 
     TeamCtl tc;
@@ -411,29 +444,36 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     GA_CUDA(cudaMemsetAsync(c->ctl.p, 0, sizeof(InstCtl), st));
     GA_CUDA(cudaMemcpyAsync(c->team.p, &c->h_team, sizeof(TeamCtl), cudaMemcpyHostToDevice, st));
     GA_CUDA(cudaMemsetAsync(P.next, 0, 16, st));
+    as.h2d += sizeof(InstDesc) + sizeof(TeamCtl);
     GA_CUDA(cudaEventRecord(c->e0, st));
     int rc = launch_search(c, kinds, P, (uint32_t)blocks, threads, smem, st);
     if (rc != GASTAR_OK) return rc;
+    ++as.launches;
     GA_CUDA(cudaEventRecord(c->e1, st));
-    if (want_path) {
-        // Arena: best + 1 states is the longest possible path; size it after
-        // reading best would need a round trip, so reserve by kind.
-        GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
-        GA_CUDA(cudaStreamSynchronize(st));
-        if (c->h_ctl->status == ST_OK) {
-            const uint64_t words = ((uint64_t)c->h_ctl->best + 2) * kw;
-            if (!c->path.ensure(words * 8 + 16)) return GASTAR_OUT_OF_MEMORY;
-            if (!c->misc.ensure(16)) return GASTAR_OUT_OF_MEMORY;
-            GA_CUDA(cudaMemsetAsync(c->misc.p, 0, 16, st));
-            rc = launch_paths(reinterpret_cast<const InstDesc*>(c->desc.p), 1,
-                              reinterpret_cast<unsigned long long*>(c->path.p), words,
-                              reinterpret_cast<unsigned long long*>(c->misc.p), st);
-            if (rc != GASTAR_OK) return rc;
-        }
-    }
     GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
     GA_CUDA(cudaStreamSynchronize(st));
-    GA_CUDA(cudaEventElapsedTime(&kernel_ms, c->e0, c->e1));
+    as.d2h += sizeof(InstCtl);
+    if (pp.kind != KIND_GRID) {
+        c->prev_slot_words = slot_words;
+        if (c->h_ctl->table_used > touched_cap) c->table_dirty = true;  // claim list overflowed
+    }
+    if (want_path && c->h_ctl->status == ST_OK) {
+        // best + 1 states is the longest possible path (every step costs >= 1).
+        const uint64_t words = ((uint64_t)c->h_ctl->best + 2) * kw;
+        if (!c->path.ensure(words * 8 + 16) || !c->misc.ensure(64)) return GASTAR_OUT_OF_MEMORY;
+        unsigned long long* used = reinterpret_cast<unsigned long long*>(c->misc.p) + 2;
+        GA_CUDA(cudaMemsetAsync(used, 0, 8, st));
+        rc = launch_paths(reinterpret_cast<const InstDesc*>(c->desc.p), 1,
+                          reinterpret_cast<unsigned long long*>(c->path.p), words, used, st);
+        if (rc != GASTAR_OK) return rc;
+        ++as.launches;
+        GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
+        GA_CUDA(cudaStreamSynchronize(st));
+        as.d2h += sizeof(InstCtl);
+    }
+    float ms = 0;
+    GA_CUDA(cudaEventElapsedTime(&ms, c->e0, c->e1));
+    as.kernel_ms += ms;
     ctl_out = *c->h_ctl;
     return GASTAR_OK;
 }
@@ -451,20 +491,17 @@ int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user
     uint64_t heap_entries = cfg.heap_entries;
     if (!heap_entries)
         heap_entries = pp.kind == KIND_GRID ? std::max<uint64_t>(1 << 20, (uint64_t)pp.W * pp.H)
-                                            : (1ull << table_log2);
+                                            : std::min<uint64_t>(1ull << table_log2, 1ull << 24);
     InstCtl ctl;
-    float ms = 0;
-    float total_ms = 0;
+    AttemptStats as;
     uint32_t attempts = 0;
     for (;;) {
         ++attempts;
-        int rc = plain_attempt(c, pp, cfg, table_log2, heap_entries, path_keys != nullptr, st, ctl, ms);
+        int rc = plain_attempt(c, pp, cfg, table_log2, heap_entries, path_keys != nullptr, st, ctl, as);
         if (rc != GASTAR_OK) return rc;
-        total_ms += ms;
-        if (!cfg.regrow && user_cfg) break;
+        if (!cfg.regrow) break;
         if (ctl.status == ST_TABLE_FULL && pp.kind != KIND_GRID && table_log2 < max_log2) {
             ++table_log2;
-            heap_entries = std::max<uint64_t>(heap_entries, 1ull << table_log2);
             continue;
         }
         if (ctl.status == ST_HEAP_FULL && heap_entries < (1ull << 32)) {
@@ -474,8 +511,12 @@ int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user
         break;
     }
     fill_result(out, ctl);
-    out->kernel_ms = total_ms;
+    out->kernel_ms = as.kernel_ms;
     out->attempts = attempts;
+    out->launches = as.launches;
+    out->h2d_bytes = as.h2d;
+    out->d2h_bytes = as.d2h;
+    c->launches += as.launches;
     if (path_keys && ctl.status == ST_OK) {
         const uint32_t kw = key_words(pp.kind);
         path_keys->resize((size_t)ctl.path_len * kw);
@@ -483,6 +524,7 @@ int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user
                                 reinterpret_cast<unsigned long long*>(c->path.p) + ctl.path_off,
                                 path_keys->size() * 8, cudaMemcpyDeviceToHost, st));
         GA_CUDA(cudaStreamSynchronize(st));
+        out->d2h_bytes += path_keys->size() * 8;
     }
     return GASTAR_OK;
 }
@@ -601,8 +643,10 @@ int gastar_solve_grid(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weig
     if (!c->weights.ensure(cells)) return GASTAR_OUT_OF_MEMORY;
     if (!cuda_ok(cudaMemcpyAsync(c->weights.p, weights, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
         return GASTAR_CUDA_ERROR;
-    return solve_grid_impl(c, w, h, reinterpret_cast<const uint8_t*>(c->weights.p), minw, sx, sy, tx,
-                           ty, cfg, path, path_cap, out, t0);
+    int rc = solve_grid_impl(c, w, h, reinterpret_cast<const uint8_t*>(c->weights.p), minw, sx, sy, tx,
+                             ty, cfg, path, path_cap, out, t0);
+    out->h2d_bytes += cells;
+    return rc;
 }
 
 int gastar_solve_grid_device(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* d_weights,

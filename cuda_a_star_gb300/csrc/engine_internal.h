@@ -15,6 +15,7 @@ namespace gastar {
 struct DevBuf {
     void* p = nullptr;
     size_t n = 0;
+    bool fresh = false;         // set when ensure() reallocated (contents undefined)
     bool ensure(size_t bytes);  // grows (contents are not kept)
     void release();
 };
@@ -53,7 +54,10 @@ struct gastar_ctx {
     char name[256] = {0};
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    gastar::DevBuf table, heaps, hdr, stage, desc, ctl, team, path, misc, weights;
+    gastar::DevBuf table, dense, touched, heaps, hdr, stage, desc, ctl, team, path, misc, weights;
+    bool table_dirty = true;       // hash table needs a full clear before the next solve
+    uint32_t prev_slot_words = 2;  // slot width of the solve that filled the touched list
+    uint64_t launches = 0;         // kernels launched by this context
     gastar::InstCtl* h_ctl = nullptr;  // pinned
     gastar::InstDesc h_desc;
     gastar::TeamCtl h_team;

@@ -40,8 +40,15 @@ struct alignas(16) InstDesc {
     uint32_t heap_cap, ew;                  // nodes per warp-heap; pops per heap per iteration
     uint64_t max_exp;                       // expansion budget (0 = none)
     uint64_t timeout_ns;                    // device deadline relative to t_start (0 = none)
-    uint32_t max_iter, pad0;                // iteration budget
+    uint32_t max_iter, delta;               // iteration budget; pop window f <= fmin + delta (0 = off)
     InstCtl* ctl;
+    // Reusable hash tables (plain engine): word offsets of the slots claimed by
+    // the previous solve, cleared at the start of the next one instead of the
+    // whole table.  touched == nullptr -> the whole table is cleared.
+    uint32_t* touched;
+    unsigned long long* touched_count;
+    uint64_t touched_cap;
+    uint32_t prev_slot_words, pad1;
 };
 
 struct alignas(16) TeamSlot {

@@ -112,9 +112,10 @@ template <int N> struct SlidingDom {
         if constexpr (KW == 1) return tab_get(t, k);
         else return tab_get(t, uint64_t(k), uint64_t(k >> 64));
     }
-    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old) {
-        if constexpr (KW == 1) return tab_insert(t, k, v, old);
-        else return tab_insert(t, uint64_t(k), uint64_t(k >> 64), v, old);
+    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
+                                                 uint64_t& slot) {
+        if constexpr (KW == 1) return tab_insert(t, k, v, old, slot);
+        else return tab_insert(t, uint64_t(k), uint64_t(k >> 64), v, old, slot);
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
     static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
@@ -197,8 +198,10 @@ struct GridDom {
     }
     static __device__ __forceinline__ Tab make_tab(const InstDesc& d) { return Tab{d.table}; }
     static __device__ __forceinline__ uint64_t get(const Tab& t, KeyT k) { return __ldcg(t.v + k); }
-    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old) {
+    static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
+                                                 uint64_t& slot) {
         old = atomicMin(t.v + k, v);
+        slot = k;
         return old == kEmpty ? 1 : 0;
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
@@ -334,14 +337,24 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
     }
     uint32_t status = kInf;  // kInf while running / suspended
     if (life == LIFE_FRESH) {
-        // Clear the table (0xff = empty key and value) across the whole team.
-        uint4* tp = reinterpret_cast<uint4*>(d.table);
-        const uint64_t n16 = d.table_words / 2;
+        // Clear the table (0xff = empty key and value) across the whole team:
+        // only the slots the previous solve claimed when they were recorded,
+        // otherwise the whole table.
         const uint64_t stride = (uint64_t)P.team_ctas * blockDim.x;
-        for (uint64_t i = (uint64_t)rank * blockDim.x + threadIdx.x; i < n16; i += stride)
-            __stcg(tp + i, make_uint4(~0u, ~0u, ~0u, ~0u));
-        if ((d.table_words & 1) && rank == 0 && threadIdx.x == 0)  // odd cell count: last word
-            __stcg(d.table + d.table_words - 1, kEmpty);
+        const uint64_t tid = (uint64_t)rank * blockDim.x + threadIdx.x;
+        if (d.touched) {
+            const uint64_t cnt = ld_vol64(d.touched_count);
+            for (uint64_t i = tid; i < cnt; i += stride) {
+                const uint64_t w = __ldcg(d.touched + i);
+                for (uint32_t j = 0; j < d.prev_slot_words; ++j) __stcg(d.table + w + j, kEmpty);
+            }
+        } else {
+            uint4* tp = reinterpret_cast<uint4*>(d.table);
+            const uint64_t n16 = d.table_words / 2;
+            for (uint64_t i = tid; i < n16; i += stride) __stcg(tp + i, make_uint4(~0u, ~0u, ~0u, ~0u));
+            if ((d.table_words & 1) && tid == 0)  // odd cell count: last word
+                __stcg(d.table + d.table_words - 1, kEmpty);
+        }
         heap_init(hp);
         if (!tsync()) status = ST_BARRIER;
         if (hid == 0) {
@@ -352,8 +365,12 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
             hp.pc = 1;
         }
         if (leader) {
-            uint64_t old;
-            D::insert(tab, ctx.start, make_val(0, kRootMove), old);
+            uint64_t old, slot = 0;
+            D::insert(tab, ctx.start, make_val(0, kRootMove), old, slot);
+            if (d.touched) {
+                *d.touched_count = 1;
+                d.touched[0] = (uint32_t)slot;
+            }
             atomicAdd(&ctl->table_used, 1ull);
             ctl->t_start = globaltimer_ns();
         }
@@ -365,6 +382,7 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
     if (status == kInf && !tsync()) status = ST_BARRIER;
 
     const uint32_t ew = d.ew;
+    uint32_t fmin = d.f0;  // min f over the open list after the previous iteration
     uint32_t it = 0;
     const uint32_t it0 = ld_vol(&ctl->iterations);
     while (status == kInf) {
@@ -374,7 +392,12 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
 
         // ---- pop + expand + insert-or-min ----
         E e;
-        const uint32_t cnt = heap_pop(hp, ew, e, lane);
+        // Pop window: with delta set, only entries with f <= fmin + delta are
+        // expanded (delta-stepping); the rest wait for later iterations.
+        const uint64_t lim = (d.delta && (uint64_t)fmin + d.delta < 0xffffffffull)
+                                 ? ((uint64_t)(fmin + d.delta + 1) << 32)
+                                 : kInfPrio;
+        const uint32_t cnt = heap_pop(hp, ew, lim, e, lane);
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
@@ -400,7 +423,8 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
 #pragma unroll
         for (int m = 0; m < D::MAXN; ++m) {
             E out = inf_entry<KW>();
-            bool acc = false;
+            bool acc = false, claimed = false;
+            uint64_t cslot = 0;
             if (act) {
                 KeyT nk;
                 uint32_t ng, nh;
@@ -408,12 +432,14 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
                     ++n_gen;
                     const uint32_t nf = ng + nh;
                     if (nf < rb) {
-                        uint64_t old;
-                        const int r = D::insert(tab, nk, make_val(ng, (uint32_t)m), old);
+                        uint64_t old, slot = 0;
+                        const int r = D::insert(tab, nk, make_val(ng, (uint32_t)m), old, slot);
                         if (r < 0) {
                             tfull = true;
                         } else {
                             n_claim += (uint32_t)r;
+                            claimed = r == 1;
+                            cslot = slot;
                             if ((uint32_t)(old >> 32) > ng) {
                                 acc = true;
                                 out.prio = make_prio(nf, ng);
@@ -422,6 +448,17 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
                             }
                         }
                     }
+                }
+            }
+            if (d.touched) {  // record claimed slots for the next solve's clear
+                const unsigned bc = __ballot_sync(kFull, claimed);
+                if (bc) {
+                    const int ldr = __ffs(bc) - 1;
+                    unsigned long long base = 0;
+                    if (lane == ldr) base = atomicAdd(d.touched_count, (unsigned long long)__popc(bc));
+                    base = __shfl_sync(kFull, base, ldr);
+                    const unsigned long long at = base + __popc(bc & ((1u << lane) - 1u));
+                    if (claimed && at < d.touched_cap) d.touched[at] = (uint32_t)cslot;
                 }
             }
             const unsigned bal = __ballot_sync(kFull, acc);
@@ -493,6 +530,7 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
         const uint32_t err = ld_vol(&S->err);
         const uint64_t gm = ld_vol64(&S->minprio);
         const uint32_t best = sm.run_best;
+        fmin = prio_f(gm);
         ++it;
         // Termination (a_star.h:260-262): best goal cost <= min f of the open list.
         // An iteration that lost entries (full table or heap) cannot prove optimality.

@@ -66,7 +66,7 @@ typedef struct gastar_config {
     uint32_t max_iterations;   /* 0 = unlimited */
     uint32_t timeout_ms;       /* device-side deadline, 0 = none */
     uint32_t regrow;           /* plain engine: re-run with doubled capacity on *_FULL (default 1) */
-    uint32_t reserved;
+    uint32_t delta;            /* pop window: expand only f <= min f + delta (0 = no window) */
     void *stream;              /* cudaStream_t to launch on (NULL = the context's stream) */
 } gastar_config;
 
@@ -84,7 +84,9 @@ typedef struct gastar_result {
     float kernel_ms;           /* device time of the search kernel(s), CUDA events */
     float total_ms;            /* host wall time of the call */
     uint32_t attempts;         /* plain engine: solves run (1 + regrows) */
-    uint32_t reserved;
+    uint32_t launches;         /* kernels this call launched */
+    uint64_t h2d_bytes;        /* bytes copied host -> device by this call */
+    uint64_t d2h_bytes;        /* bytes copied device -> host by this call */
 } gastar_result;
 
 typedef struct gastar_ctx gastar_ctx;
