@@ -255,6 +255,21 @@ def run_ours(args) -> dict:
     return out if rank == 0 else {}
 
 
+def run_profile_case() -> None:
+    """A small copy of the workload for ncu captures (a few GB on the device):
+    4 of the 64 instances, 2^24-slot table, one pass."""
+    import cuda_a_star_gb300 as g
+    from cuda_a_star_gb300 import build as engine_build
+    engine_build.build()
+    with g.Engine(0) as eng:
+        cfg = g.make_config(num_queues=WORKLOAD["num_queues"], table_log2=24)
+        for s, goal in _instances(g)[:4]:
+            r = eng.solve_sliding(s, goal, WORKLOAD["n"], config=cfg, path=True, path_cap=1024)
+            print(json.dumps({"status": r.status_name, "cost": r.cost, "expansions": r.expansions,
+                              "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
+                              "kernel_ms": r.kernel_ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -262,7 +277,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small single pass for ncu captures (no JSON line)")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case()
+        return
     rank, world = _dist()
     if args.impl == "reference":
         if rank != 0:

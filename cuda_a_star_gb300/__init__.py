@@ -18,7 +18,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BatchConfig, Config, Result
+from ._lib import BatchConfig, Config, Result  # noqa: F401  (re-exported)
 
 H_ADMISSIBLE, H_REFERENCE, H_ZERO = 0, 1, 2
 MOVES_STANDARD, MOVES_REFERENCE = 0, 1
