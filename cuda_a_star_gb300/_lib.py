@@ -17,6 +17,7 @@ EXPORTS = [
     "gastar_config_default", "gastar_create", "gastar_destroy", "gastar_last_error",
     "gastar_status_name", "gastar_version", "gastar_device_info",
     "gastar_solve_sliding", "gastar_solve_grid", "gastar_solve_grid_device",
+    "gastar_solve_sliding_noalloc",
     "gastar_batch_config_default", "gastar_batch_create", "gastar_batch_destroy",
     "gastar_batch_add_sliding", "gastar_batch_add_grid", "gastar_batch_run",
     "gastar_batch_rerun", "gastar_batch_count", "gastar_batch_result", "gastar_batch_path",
@@ -82,6 +83,8 @@ def load(path: str | None = None) -> C.CDLL:
                                          C.c_char_p, C.c_size_t]),
         "gastar_solve_sliding": (C.c_int, [vp, C.c_uint32, u8p, u8p, C.POINTER(Config), u8p,
                                            C.c_uint32, C.POINTER(Result)]),
+        "gastar_solve_sliding_noalloc": (C.c_int, [C.c_uint32, u8p, u8p, C.POINTER(Config), u8p,
+                                                   C.c_uint32, C.POINTER(Result)]),
         "gastar_solve_grid": (C.c_int, [vp, C.c_uint32, C.c_uint32, u8p, C.c_uint32, C.c_uint32,
                                         C.c_uint32, C.c_uint32, C.POINTER(Config), u32p,
                                         C.c_uint32, C.POINTER(Result)]),

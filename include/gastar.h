@@ -123,6 +123,19 @@ int gastar_solve_grid_device(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint
                              const gastar_config *cfg, uint32_t *path, uint32_t path_cap,
                              gastar_result *out);
 
+/* 8-puzzle solve that allocates nothing, for callers that cannot call
+ * cudaMalloc (their device memory is reserved by another pool, or they must
+ * avoid the device-wide synchronisation of cudaMalloc/cudaFree).  No
+ * counterpart in the reference.  Same arguments and results as
+ * gastar_solve_sliding without a context; n must be 3 (GASTAR_BAD_INPUT
+ * otherwise).  Scratch is a fixed ~16 MiB device array inside the library,
+ * held by every GPU that loads the library until exit; all calls share it, so
+ * calls that overlap on the GPU race.  The first call on a device looks up the
+ * array's address: make it before any stream capture.  kernel_ms is 0. */
+int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t *start, const uint8_t *goal,
+                                 const gastar_config *cfg, uint8_t *path, uint32_t path_cap,
+                                 gastar_result *out);
+
 /* ---- batched GA*: many instances in one persistent launch ----
  * No reference counterpart (the reference solves one instance per process,
  * its problem data lives in __constant__ symbols: a_star_sliding_puzzle.h:125-128,
