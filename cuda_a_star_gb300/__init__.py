@@ -18,7 +18,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BatchConfig, Config, Result  # noqa: F401  (re-exported)
+from ._lib import BatchConfig, Config, Result, ServeConfig  # noqa: F401  (re-exported)
 
 H_ADMISSIBLE, H_REFERENCE, H_ZERO = 0, 1, 2
 MOVES_STANDARD, MOVES_REFERENCE = 0, 1
@@ -164,6 +164,9 @@ class Engine:
     def batch(self, **kw) -> "Batch":
         return Batch(self, **kw)
 
+    def server(self, **kw) -> "Server":
+        return Server(self, **kw)
+
 
 class Batch:
     """Many instances solved by one persistent launch (see gastar_batch_*)."""
@@ -241,6 +244,105 @@ class Batch:
         lib().gastar_batch_stats(self._h, C.byref(ms), C.byref(h2d), C.byref(d2h), C.byref(dev))
         return {"kernel_ms": ms.value, "h2d_bytes": h2d.value, "d2h_bytes": d2h.value,
                 "device_bytes": dev.value}
+
+
+class Server:
+    """Continuous-batching request loop (see gastar_serve_*)."""
+
+    PENDING = 11
+
+    def __init__(self, engine: Engine, **kw):
+        cfg = ServeConfig()
+        lib().gastar_serve_config_default(C.byref(cfg))
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        self._h = lib().gastar_serve_create(engine._h, C.byref(cfg))
+        if not self._h:
+            raise GastarError("gastar_serve_create: " + lib().gastar_last_error().decode())
+        engine._batches.add(self)
+        self.kinds: dict[int, tuple] = {}
+
+    def close(self):
+        if self._h:
+            lib().gastar_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit_sliding(self, start, goal) -> int:
+        s = np.ascontiguousarray(start, dtype=np.uint8).reshape(-1)
+        g = np.ascontiguousarray(goal, dtype=np.uint8).reshape(-1)
+        n = int(round(len(s) ** 0.5))
+        i = lib().gastar_serve_submit_sliding(self._h, n, _u8p(s), _u8p(g))
+        if i < 0:
+            _check(-i, "gastar_serve_submit_sliding")
+        self.kinds[i] = ("sliding", n)
+        return i
+
+    def submit_grid(self, weights, start, goal) -> int:
+        w8 = np.ascontiguousarray(weights, dtype=np.uint8)
+        h, w = w8.shape
+        i = lib().gastar_serve_submit_grid(self._h, w, h, _u8p(w8), start[0], start[1], goal[0],
+                                           goal[1])
+        if i < 0:
+            _check(-i, "gastar_serve_submit_grid")
+        self.kinds[i] = ("grid", w * h)
+        return i
+
+    def step(self) -> None:
+        _check(lib().gastar_serve_step(self._h), "gastar_serve_step")
+
+    def poll(self, i: int, path: bool = True) -> SolveResult | None:
+        r = Result()
+        rc = lib().gastar_serve_poll(self._h, i, C.byref(r), None, 0, None)
+        if rc == self.PENDING:
+            return None
+        _check(rc, "gastar_serve_poll")
+        p = None
+        if path and r.status == OK:
+            kind, size = self.kinds[i]
+            buf = (np.zeros(r.path_len, dtype=np.uint32) if kind == "grid"
+                   else np.zeros((r.path_len, size * size), dtype=np.uint8))
+            ln = C.c_uint32()
+            _check(lib().gastar_serve_poll(self._h, i, C.byref(r), buf.ctypes.data_as(C.c_void_p),
+                                           r.path_len, C.byref(ln)), "gastar_serve_poll")
+            p = buf
+        return SolveResult.from_c(r, p)
+
+    def release(self, i: int) -> None:
+        lib().gastar_serve_release(self._h, i)
+        self.kinds.pop(i, None)
+
+    def stats(self) -> dict:
+        wt, ac = C.c_uint32(), C.c_uint32()
+        done, used = C.c_uint64(), C.c_uint64()
+        ms = C.c_float()
+        lib().gastar_serve_stats(self._h, C.byref(wt), C.byref(ac), C.byref(done), C.byref(used),
+                                 C.byref(ms))
+        return {"waiting": wt.value, "active": ac.value, "completed": done.value,
+                "bytes_in_use": used.value, "kernel_ms": ms.value}
+
+    def drain(self, ids, max_steps: int = 1_000_000) -> dict:
+        """Steps until every id in `ids` is finished; returns id -> SolveResult."""
+        out = {}
+        pending = set(ids)
+        for _ in range(max_steps):
+            if not pending:
+                break
+            self.step()
+            for i in list(pending):
+                r = self.poll(i)
+                if r is not None:
+                    out[i] = r
+                    pending.discard(i)
+        if pending:
+            raise GastarError(f"{len(pending)} requests still pending")
+        return out
 
 
 # ---- host-only helpers (no GPU needed) ----

@@ -22,6 +22,9 @@ EXPORTS = [
     "gastar_batch_add_sliding", "gastar_batch_add_grid", "gastar_batch_run",
     "gastar_batch_rerun", "gastar_batch_count", "gastar_batch_result", "gastar_batch_path",
     "gastar_batch_stats",
+    "gastar_serve_config_default", "gastar_serve_create", "gastar_serve_destroy",
+    "gastar_serve_submit_sliding", "gastar_serve_submit_grid", "gastar_serve_step",
+    "gastar_serve_poll", "gastar_serve_release", "gastar_serve_stats",
     "gastar_parse_sliding", "gastar_format_sliding", "gastar_parse_grid_dims",
     "gastar_parse_grid", "gastar_gen_sliding", "gastar_gen_grid",
 ]
@@ -54,6 +57,17 @@ class BatchConfig(C.Structure):
         ("load_factor", C.c_float), ("heuristic", C.c_uint32), ("moves", C.c_uint32),
         ("use_graph", C.c_uint32), ("blocks", C.c_uint32), ("timeout_ms", C.c_uint32),
         ("max_expansions", C.c_uint64), ("sliding_states", C.c_uint64),
+        ("delta_grid", C.c_uint32), ("heavy_team", C.c_uint32), ("heavy_cells", C.c_uint64),
+        ("promote_expansions", C.c_uint64),
+    ]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("slice_iters", C.c_uint32),
+        ("warps_per_block", C.c_uint32), ("expansion_width", C.c_uint32),
+        ("load_factor", C.c_float), ("heuristic", C.c_uint32), ("moves", C.c_uint32),
+        ("delta_grid", C.c_uint32), ("sliding_states", C.c_uint64),
     ]
 
 
@@ -105,6 +119,17 @@ def load(path: str | None = None) -> C.CDLL:
         "gastar_batch_path": (C.c_int, [vp, C.c_uint32, vp, C.c_uint32, u32p]),
         "gastar_batch_stats": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "gastar_serve_config_default": (None, [C.POINTER(ServeConfig)]),
+        "gastar_serve_create": (vp, [vp, C.POINTER(ServeConfig)]),
+        "gastar_serve_destroy": (None, [vp]),
+        "gastar_serve_submit_sliding": (C.c_int64, [vp, C.c_uint32, u8p, u8p]),
+        "gastar_serve_submit_grid": (C.c_int64, [vp, C.c_uint32, C.c_uint32, u8p, C.c_uint32,
+                                                 C.c_uint32, C.c_uint32, C.c_uint32]),
+        "gastar_serve_step": (C.c_int, [vp]),
+        "gastar_serve_poll": (C.c_int, [vp, C.c_int64, C.POINTER(Result), vp, C.c_uint32, u32p]),
+        "gastar_serve_release": (C.c_int, [vp, C.c_int64]),
+        "gastar_serve_stats": (C.c_int, [vp, u32p, u32p, C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
         "gastar_parse_sliding": (C.c_int, [C.c_char_p, C.c_uint32, u8p, u8p]),
         "gastar_format_sliding": (C.c_int, [C.c_uint32, u8p, C.c_char_p, C.c_size_t]),
         "gastar_parse_grid_dims": (C.c_int, [C.c_char_p, u32p, u32p]),

@@ -19,6 +19,7 @@
 #include "../../include/gastar.h"
 #include "device_common.cuh"
 #include "engine_internal.h"
+#include "partition.h"
 
 namespace gastar {
 
@@ -54,19 +55,19 @@ int device_min_weight(gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStr
 
 using namespace gastar;
 
-struct BatchInst {
-    uint32_t kind, n;
-    uint64_t start0, start1, goal0, goal1;
-    uint32_t W, H, minw, f0;
-    std::vector<uint8_t> weights;  // grid
-    uint64_t weights_off = 0;
-    uint64_t est = 0;              // scheduling estimate (larger first)
-};
-
 struct gastar_batch {
     gastar_ctx* ctx = nullptr;
     gastar_batch_config cfg;
-    std::vector<BatchInst> insts;
+    std::vector<Problem> insts;
+    std::vector<uint64_t> weights_off;
+    std::vector<uint8_t> heavy;        // solved by a multi-block team
+    std::vector<uint8_t> promotable;   // re-solved by the plain engine past the budget
+    uint32_t n_heavy = 0, heavy_teams = 0;
+    uint64_t heavy_stage_bytes = 0;
+    DevBuf team_ctl, team_stage;
+    uint32_t promoted = 0;
+    uint32_t retry_level = 0;   // partitions scale by 4^retry_level
+    uint32_t retried = 0;       // instances re-solved with larger partitions in the last run
     bool uploaded = false;
     DevBuf arena, weights, descs, ctls, order, counters, paths;
     std::vector<InstDesc> h_desc;
@@ -91,6 +92,10 @@ void gastar_batch_config_default(gastar_batch_config* cfg) {
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
     cfg->use_graph = 1;
+    cfg->delta_grid = 36;
+    cfg->heavy_team = 4;
+    cfg->heavy_cells = 1ull << 20;
+    cfg->promote_expansions = 1ull << 21;
 }
 
 gastar_batch* gastar_batch_create(gastar_ctx* c, const gastar_batch_config* cfg) {
@@ -99,6 +104,7 @@ gastar_batch* gastar_batch_create(gastar_ctx* c, const gastar_batch_config* cfg)
     b->ctx = c;
     if (cfg) b->cfg = *cfg;
     else gastar_batch_config_default(&b->cfg);
+    if (!b->cfg.heavy_team) b->cfg.heavy_team = 1;
     if (!b->cfg.warps_per_block) b->cfg.warps_per_block = 8;
     if (!b->cfg.expansion_width) b->cfg.expansion_width = 32;
     if (b->cfg.load_factor <= 0.f) b->cfg.load_factor = 0.75f;
@@ -122,6 +128,8 @@ void gastar_batch_destroy(gastar_batch* b) {
     b->order.release();
     b->counters.release();
     b->paths.release();
+    b->team_ctl.release();
+    b->team_stage.release();
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
@@ -130,47 +138,24 @@ void gastar_batch_destroy(gastar_batch* b) {
 
 int gastar_batch_add_sliding(gastar_batch* b, uint32_t n, const uint8_t* start, const uint8_t* goal) {
     if (!b || b->uploaded) return -GASTAR_BAD_INPUT;
-    if (!valid_board(n, start) || !valid_board(n, goal)) {
+    Problem p;
+    if (!make_sliding_problem(n, start, goal, b->cfg.heuristic, b->cfg.moves, p)) {
         set_error("sliding: boards must be permutations of 0..n*n-1 with n in 3..5");
         return -GASTAR_BAD_INPUT;
     }
-    BatchInst in;
-    in.kind = n == 3 ? KIND_SLIDING3 : n == 4 ? KIND_SLIDING4 : KIND_SLIDING5;
-    in.n = n;
-    pack_board(n, start, in.start0, in.start1);
-    pack_board(n, goal, in.goal0, in.goal1);
-    in.W = in.H = in.minw = 0;
-    in.f0 = sliding_h(n, start, goal, b->cfg.heuristic);
-    // Unsolvable (other parity class): mark with est = 0 and f0 = ~0.
-    if (b->cfg.moves == GASTAR_MOVES_STANDARD && !sliding_solvable(n, start, goal)) in.f0 = kInf;
-    in.est = (uint64_t)in.f0 * (n == 5 ? 4 : n == 4 ? 2 : 1);
-    b->insts.push_back(std::move(in));
+    b->insts.push_back(std::move(p));
     return (int)b->insts.size() - 1;
 }
 
 int gastar_batch_add_grid(gastar_batch* b, uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx,
                           uint32_t sy, uint32_t tx, uint32_t ty) {
     if (!b || b->uploaded) return -GASTAR_BAD_INPUT;
-    if (!weights || !w || !h || w > 65535 || h > 65535 || sx >= w || sy >= h || tx >= w || ty >= h) {
+    Problem p;
+    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, b->cfg.heuristic, p)) {
         set_error("grid: bad dimensions or endpoints");
         return -GASTAR_BAD_INPUT;
     }
-    BatchInst in;
-    in.kind = KIND_GRID;
-    in.n = 0;
-    in.W = w;
-    in.H = h;
-    in.start0 = (uint64_t)sy * w + sx;
-    in.goal0 = (uint64_t)ty * w + tx;
-    in.start1 = in.goal1 = 0;
-    in.weights.assign(weights, weights + (size_t)w * h);
-    uint32_t minw = 255;
-    for (uint8_t v : in.weights)
-        if (v && v < minw) minw = v;
-    in.minw = minw;
-    in.f0 = grid_h(sx, sy, tx, ty, minw, b->cfg.heuristic);
-    in.est = 1000000ull + (uint64_t)w * h;
-    b->insts.push_back(std::move(in));
+    b->insts.push_back(std::move(p));
     return (int)b->insts.size() - 1;
 }
 
@@ -180,78 +165,81 @@ uint32_t gastar_batch_count(const gastar_batch* b) { return b ? (uint32_t)b->ins
 
 namespace {
 
+PartConfig part_config(const gastar_batch* b) {
+    PartConfig pc;
+    const auto& cf = b->cfg;
+    pc.warps = cf.warps_per_block;
+    pc.ew = cf.expansion_width;
+    pc.load_factor = cf.load_factor;
+    pc.heuristic = cf.heuristic;
+    pc.moves = cf.moves;
+    pc.delta_grid = cf.delta_grid;
+    pc.sliding_states = cf.sliding_states;
+    pc.max_exp = cf.max_expansions;
+    pc.timeout_ms = cf.timeout_ms;
+    pc.retry_level = b->retry_level;
+    return pc;
+}
+
 int batch_upload(gastar_batch* b) {
     gastar_ctx* c = b->ctx;
     const uint32_t n = (uint32_t)b->insts.size();
-    const auto& cf = b->cfg;
-    const uint32_t W = cf.warps_per_block, ew = cf.expansion_width;
-    b->threads = W * 32;
-    uint32_t kinds = 0;
-    for (auto& in : b->insts) kinds |= kind_bit(in.kind);
-    b->smem = stage_smem_bytes(kKindsAll, W, ew);
+    const PartConfig pc = part_config(b);
+    b->threads = pc.warps * 32;
+    b->smem = block_smem_bytes(kKindsAll, pc.warps, pc.ew, false);
     const int nb = occupancy_blocks(c, kKindsAll, b->threads, b->smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
-    b->blocks = cf.blocks ? cf.blocks : (uint32_t)(nb * c->sms);
+    b->blocks = b->cfg.blocks ? b->cfg.blocks : (uint32_t)(nb * c->sms);
     b->blocks = std::max(1u, std::min(b->blocks, n));
 
-    // Partition sizes.
-    const float lf = std::min(0.95f, std::max(0.1f, cf.load_factor));
-    b->h_desc.assign(n, InstDesc());
-    std::vector<uint64_t> part_off(n), part_bytes(n);
+    // Heavy instances (large grids) are solved by teams of heavy_team blocks;
+    // their partitions hold heavy_team x warps warp-heaps.
+    const uint32_t T = std::max(1u, b->cfg.heavy_team);
+    PartConfig pch = pc;
+    pch.warps = pc.warps * T;
+    b->heavy.assign(n, 0);
+    b->promotable.assign(n, 0);
+    b->n_heavy = 0;
+    uint64_t heavy_est = 0, total_est = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const Problem& p = b->insts[i];
+        const uint64_t work = p.kind == KIND_GRID ? (uint64_t)p.W * p.H : (1ull << 16);
+        total_est += work;
+        if (T > 1 && p.kind == KIND_GRID && (uint64_t)p.W * p.H >= b->cfg.heavy_cells) {
+            b->heavy[i] = 1;
+            ++b->n_heavy;
+            heavy_est += work;
+        }
+        const uint64_t pe = b->cfg.promote_expansions;
+        if (p.kind != KIND_GRID && p.n >= 4 && pe && (!b->cfg.max_expansions || b->cfg.max_expansions > pe))
+            b->promotable[i] = 1;
+    }
+    b->heavy_teams = 0;
+    if (b->n_heavy) {
+        const double share = total_est ? (double)heavy_est / (double)total_est : 1.0;
+        b->heavy_teams = (uint32_t)std::max<double>(1.0, share * b->blocks / T + 0.5);
+        b->heavy_teams = std::min(b->heavy_teams, b->n_heavy);
+        b->heavy_teams = std::min(b->heavy_teams, b->blocks / T);
+        if (b->heavy_teams == 0) {  // too few blocks for a team: no teams
+            b->n_heavy = 0;
+            std::fill(b->heavy.begin(), b->heavy.end(), 0);
+        }
+    }
+    std::vector<PartPlan> plans(n);
+    std::vector<uint64_t> part_off(n);
     uint64_t arena_bytes = 0, weights_bytes = 0;
     b->path_words = 0;
+    b->weights_off.assign(n, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const BatchInst& in = b->insts[i];
-        InstDesc& d = b->h_desc[i];
-        std::memset(&d, 0, sizeof(d));
-        d.kind = in.kind;
-        d.heuristic = cf.heuristic;
-        d.moves = cf.moves;
-        d.n = in.n;
-        d.start0 = in.start0;
-        d.start1 = in.start1;
-        d.goal0 = in.goal0;
-        d.goal1 = in.goal1;
-        d.W = in.W;
-        d.H = in.H;
-        d.minw = in.minw;
-        d.f0 = in.f0 == kInf ? 0 : in.f0;
-        d.heaps = W;
-        d.ew = ew;
-        d.max_probe = 4096;
-        d.max_exp = cf.max_expansions;
-        d.timeout_ns = (uint64_t)cf.timeout_ms * 1000000ull;
-        uint64_t states, table_bytes, entries;
-        const uint32_t eb = entry_bytes(in.kind);
-        if (in.kind == KIND_GRID) {
-            states = (uint64_t)in.W * in.H;
-            d.table_words = states;
-            d.table_limit = ~0ull;
-            table_bytes = states * 8;
-            entries = std::max<uint64_t>(1 << 16, states);
-            b->path_words += std::max<uint64_t>(1024, 4ull * (in.W + in.H));
-            weights_bytes = (weights_bytes + 15) & ~15ull;
-            b->insts[i].weights_off = weights_bytes;
-            weights_bytes += states;
-        } else {
-            states = cf.sliding_states ? cf.sliding_states
-                                       : (in.n == 3 ? 181440ull : (1ull << 20));
-            const uint64_t slots = next_pow2((uint64_t)((double)states / lf) + 1);
-            const uint32_t sw = key_words(in.kind) == 1 ? 2 : 4;
-            d.table_words = slots * sw;
-            d.table_mask = slots - 1;
-            d.table_limit = (uint64_t)((double)slots * lf);
-            table_bytes = d.table_words * 8;
-            entries = states;
-            b->path_words += 512ull * key_words(in.kind);
-        }
-        const uint64_t per_heap = (entries + W - 1) / W;
-        const uint64_t cap_nodes = std::max<uint64_t>(4, (per_heap * 2 + 31) / 32);
-        d.heap_cap = (uint32_t)cap_nodes;
-        const uint64_t heap_bytes = (uint64_t)W * (cap_nodes + 1) * 32 * eb;
+        plans[i] = plan_partition(b->insts[i], b->heavy[i] ? pch : pc);
         part_off[i] = arena_bytes;
-        part_bytes[i] = table_bytes + (uint64_t)W * 8 + 256 + heap_bytes;
-        arena_bytes += (part_bytes[i] + 255) & ~255ull;
+        arena_bytes += plans[i].bytes;
+        b->path_words += plans[i].path_words;
+        if (b->insts[i].kind == KIND_GRID) {
+            weights_bytes = (weights_bytes + 15) & ~15ull;
+            b->weights_off[i] = weights_bytes;
+            weights_bytes += b->insts[i].weights.size();
+        }
     }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -268,44 +256,42 @@ int batch_upload(gastar_batch* b) {
                       (sizeof(InstDesc) + sizeof(InstCtl)) * (size_t)n;
     char* base = reinterpret_cast<char*>(b->arena.p);
     InstCtl* ctl_base = reinterpret_cast<InstCtl*>(b->ctls.p);
+    b->h_desc.assign(n, InstDesc());
     for (uint32_t i = 0; i < n; ++i) {
-        InstDesc& d = b->h_desc[i];
-        char* p = base + part_off[i];
-        d.table = reinterpret_cast<unsigned long long*>(p);
-        p += d.table_words * 8;
-        d.heap_hdr = reinterpret_cast<uint32_t*>(p);
-        p += (uint64_t)W * 8;
-        p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
-        d.heap_nodes = p;
-        d.ctl = ctl_base + i;
-        if (b->insts[i].kind == KIND_GRID)
-            d.weights = reinterpret_cast<const uint8_t*>(b->weights.p) + b->insts[i].weights_off;
-    }
-    for (uint32_t i = 0; i < n; ++i) {
-        const InstDesc& d = b->h_desc[i];
-        const char* end = reinterpret_cast<const char*>(d.heap_nodes) +
-                          (uint64_t)W * (d.heap_cap + 1) * 32 * entry_bytes(d.kind);
-        if (end > base + part_off[i] + part_bytes[i]) {
-            set_error("internal: partition layout overflow");
-            return GASTAR_BAD_INPUT;
-        }
+        fill_desc(b->h_desc[i], b->insts[i], b->heavy[i] ? pch : pc, plans[i], base + part_off[i],
+                  reinterpret_cast<const uint8_t*>(b->weights.p) + b->weights_off[i], ctl_base + i);
+        if (b->promotable[i])
+            b->h_desc[i].max_exp = b->h_desc[i].max_exp ? std::min<uint64_t>(b->h_desc[i].max_exp,
+                                                                              b->cfg.promote_expansions)
+                                                        : b->cfg.promote_expansions;
     }
     // Largest estimated work first; puzzles in the other parity class of the
-    // standard move set are unreachable and are not scheduled at all.
-    std::vector<uint32_t> order;
-    for (uint32_t i = 0; i < n; ++i)
-        if (!(b->insts[i].kind != KIND_GRID && b->insts[i].f0 == kInf)) order.push_back(i);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t bb) { return b->insts[a].est > b->insts[bb].est; });
+    // standard move set are unreachable and are not scheduled at all.  The
+    // order array holds the one-block instances, then the heavy ones.
+    std::vector<uint32_t> order, horder;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->insts[i].unreachable) continue;
+        (b->heavy[i] ? horder : order).push_back(i);
+    }
+    auto by_est = [&](uint32_t a, uint32_t bb) { return b->insts[a].est > b->insts[bb].est; };
+    std::stable_sort(order.begin(), order.end(), by_est);
+    std::stable_sort(horder.begin(), horder.end(), by_est);
     b->n_sched = (uint32_t)order.size();
+    order.insert(order.end(), horder.begin(), horder.end());
+    if (b->n_heavy) {
+        b->heavy_stage_bytes = 2 * stage_entries_per_buffer(pch.warps, pch.ew, 8) * 16;
+        if (!b->team_ctl.ensure(sizeof(TeamCtl) * b->heavy_teams) ||
+            !b->team_stage.ensure(b->heavy_stage_bytes * b->heavy_teams))
+            return GASTAR_OUT_OF_MEMORY;
+    }
     if (!b->h_ctl && !cuda_ok(cudaMallocHost(&b->h_ctl, sizeof(InstCtl) * (n + 1)), "cudaMallocHost"))
         return GASTAR_CUDA_ERROR;
     cudaStream_t st = c->stream;
     b->h2d = 0;
     for (uint32_t i = 0; i < n; ++i) {
-        const BatchInst& in = b->insts[i];
+        const Problem& in = b->insts[i];
         if (in.kind != KIND_GRID) continue;
-        if (!cuda_ok(cudaMemcpyAsync(reinterpret_cast<char*>(b->weights.p) + in.weights_off,
+        if (!cuda_ok(cudaMemcpyAsync(reinterpret_cast<char*>(b->weights.p) + b->weights_off[i],
                                      in.weights.data(), in.weights.size(), cudaMemcpyHostToDevice, st),
                      "cudaMemcpyAsync"))
             return GASTAR_CUDA_ERROR;
@@ -313,8 +299,8 @@ int batch_upload(gastar_batch* b) {
     }
     if (!cuda_ok(cudaMemcpyAsync(b->descs.p, b->h_desc.data(), sizeof(InstDesc) * n,
                                  cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
-        (b->n_sched && !cuda_ok(cudaMemcpyAsync(b->order.p, order.data(), sizeof(uint32_t) * b->n_sched,
-                                                cudaMemcpyHostToDevice, st), "cudaMemcpyAsync")) ||
+        (!order.empty() && !cuda_ok(cudaMemcpyAsync(b->order.p, order.data(), sizeof(uint32_t) * order.size(),
+                                                    cudaMemcpyHostToDevice, st), "cudaMemcpyAsync")) ||
         !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
         return GASTAR_CUDA_ERROR;
     b->h2d += sizeof(InstDesc) * n + sizeof(uint32_t) * n;
@@ -323,7 +309,7 @@ int batch_upload(gastar_batch* b) {
 }
 
 // Enqueues one full solve of every instance on `st`.
-int batch_enqueue(gastar_batch* b, cudaStream_t st, bool timed) {
+int batch_enqueue(gastar_batch* b, cudaStream_t st, bool capturing) {
     const uint32_t n = (uint32_t)b->insts.size();
     unsigned long long* used = reinterpret_cast<unsigned long long*>(b->counters.p) + 1;
     if (!cuda_ok(cudaMemsetAsync(b->ctls.p, 0, sizeof(InstCtl) * (n + 1), st), "cudaMemsetAsync") ||
@@ -337,13 +323,24 @@ int batch_enqueue(gastar_batch* b, cudaStream_t st, bool timed) {
     P.next = reinterpret_cast<uint32_t*>(b->counters.p);
     P.team_ctas = 1;
     P.barrier_timeout_ns = 2000000000ull;
-    // External records stay timing events when the sequence is captured in a graph.
-    if (timed && !cuda_ok(cudaEventRecordWithFlags(b->e0, st, cudaEventRecordExternal), "cudaEventRecord"))
-        return GASTAR_CUDA_ERROR;
+    if (b->n_heavy) {
+        P.heavy_order = reinterpret_cast<const uint32_t*>(b->order.p) + b->n_sched;
+        P.n_heavy = b->n_heavy;
+        P.heavy_team = b->cfg.heavy_team;
+        P.heavy_teams = b->heavy_teams;
+        P.heavy_next = reinterpret_cast<uint32_t*>(b->counters.p) + 4;
+        P.heavy_ctl = reinterpret_cast<TeamCtl*>(b->team_ctl.p);
+        P.heavy_stage = b->team_stage.p;
+        P.heavy_stage_bytes = b->heavy_stage_bytes;
+        if (!cuda_ok(cudaMemsetAsync(b->team_ctl.p, 0, sizeof(TeamCtl) * b->heavy_teams, st), "cudaMemsetAsync"))
+            return GASTAR_CUDA_ERROR;
+    }
+    // Inside a graph capture, external records stay timing events.
+    const unsigned flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (!cuda_ok(cudaEventRecordWithFlags(b->e0, st, flags), "cudaEventRecord")) return GASTAR_CUDA_ERROR;
     int rc = launch_search(b->ctx, kKindsAll, P, b->blocks, b->threads, b->smem, st);
     if (rc != GASTAR_OK) return rc;
-    if (timed && !cuda_ok(cudaEventRecordWithFlags(b->e1, st, cudaEventRecordExternal), "cudaEventRecord"))
-        return GASTAR_CUDA_ERROR;
+    if (!cuda_ok(cudaEventRecordWithFlags(b->e1, st, flags), "cudaEventRecord")) return GASTAR_CUDA_ERROR;
     rc = launch_paths(P.insts, n, reinterpret_cast<unsigned long long*>(b->paths.p), b->path_words, used, st);
     if (rc != GASTAR_OK) return rc;
     // Control blocks and the arena fill counter come back in one copy.
@@ -375,7 +372,7 @@ int batch_finish(gastar_batch* b) {
     }
     // Instances the standard move set cannot solve never ran a search.
     for (uint32_t i = 0; i < n; ++i)
-        if (b->insts[i].kind != KIND_GRID && b->insts[i].f0 == kInf) {
+        if (b->insts[i].unreachable) {
             b->h_ctl[i].status = ST_NO_PATH;
             b->h_ctl[i].life = LIFE_DONE;
         }
@@ -397,6 +394,105 @@ int gastar_batch_run(gastar_batch* b) {
     return gastar_batch_rerun(b);
 }
 
+namespace {
+
+// Re-solves the instances whose partition overflowed (or whose path did not
+// fit the arena) in a follow-up batch with 4x larger partitions, then merges
+// their control blocks and paths back.  The follow-up batch retries its own
+// overflows the same way, down to 64x the class size.
+int batch_retry_overflows(gastar_batch* b) {
+    b->retried = 0;
+    if (b->retry_level >= 3) return GASTAR_OK;
+    const uint32_t n = (uint32_t)b->insts.size();
+    std::vector<uint32_t> bad;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t st = b->h_ctl[i].status;
+        if (st == ST_TABLE_FULL || st == ST_HEAP_FULL || st == ST_PATH_CAP) bad.push_back(i);
+    }
+    if (bad.empty()) return GASTAR_OK;
+    gastar_batch* sub = gastar_batch_create(b->ctx, &b->cfg);
+    if (!sub) return GASTAR_OUT_OF_MEMORY;
+    sub->cfg.use_graph = 0;
+    sub->retry_level = b->retry_level + 1;
+    for (uint32_t i : bad) sub->insts.push_back(b->insts[i]);
+    int rc = gastar_batch_run(sub);
+    if (rc == GASTAR_OK) {
+        b->retried = (uint32_t)bad.size();
+        for (size_t j = 0; j < bad.size(); ++j) {
+            InstCtl c = sub->h_ctl[j];
+            c.iterations += b->h_ctl[bad[j]].iterations;
+            c.expansions += b->h_ctl[bad[j]].expansions;
+            if (c.status == ST_OK) {
+                const uint64_t words = (uint64_t)c.path_len * key_words(b->insts[bad[j]].kind);
+                const uint64_t off = b->h_paths.size();
+                b->h_paths.insert(b->h_paths.end(), sub->h_paths.begin() + c.path_off,
+                                  sub->h_paths.begin() + c.path_off + words);
+                c.path_off = off;
+            }
+            b->h_ctl[bad[j]] = c;
+        }
+        b->kernel_ms += sub->kernel_ms;
+        b->h2d += sub->h2d;
+        b->d2h += sub->d2h;
+    }
+    gastar_batch_destroy(sub);
+    return rc;
+}
+
+}  // namespace
+
+// Puzzles that used up their promotion budget in the batch are solved again
+// from scratch by the plain engine: one instance on every block of the GPU.
+static int batch_promote(gastar_batch* b) {
+    b->promoted = 0;
+    const uint32_t n = (uint32_t)b->insts.size();
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!b->promotable[i] || b->h_ctl[i].status != ST_BUDGET) continue;
+        const Problem& p = b->insts[i];
+        PlainProblem pp;
+        std::memset(&pp, 0, sizeof(pp));
+        pp.kind = p.kind;
+        pp.n = p.n;
+        pp.start0 = p.start0;
+        pp.start1 = p.start1;
+        pp.goal0 = p.goal0;
+        pp.goal1 = p.goal1;
+        pp.f0 = p.f0;
+        gastar_config cfg;
+        gastar_config_default(&cfg);
+        cfg.num_queues = 16384;
+        cfg.heuristic = b->cfg.heuristic;
+        cfg.moves = b->cfg.moves;
+        cfg.timeout_ms = b->cfg.timeout_ms;
+        if (b->cfg.max_expansions) cfg.max_expansions = b->cfg.max_expansions;
+        std::vector<uint64_t> keys;
+        gastar_result r;
+        std::memset(&r, 0, sizeof(r));
+        const int rc = plain_solve(b->ctx, pp, &cfg, &keys, &r);
+        if (rc != GASTAR_OK) return rc;
+        InstCtl& c = b->h_ctl[i];
+        const uint64_t batch_exp = c.expansions, t0 = c.t_start;
+        c.status = (uint32_t)r.status;
+        c.best = r.cost;
+        c.path_len = r.status == GASTAR_OK ? r.path_len : 0;
+        c.iterations += r.iterations;
+        c.expansions = batch_exp + r.expansions;
+        c.generated += r.generated;
+        c.pushes += r.pushes;
+        c.stale += r.stale;
+        c.table_used = r.table_used;
+        c.t_end = c.t_end + (uint64_t)((double)r.kernel_ms * 1e6);
+        c.t_start = t0;
+        if (r.status == GASTAR_OK) {
+            c.path_off = b->h_paths.size();
+            b->h_paths.insert(b->h_paths.end(), keys.begin(), keys.end());
+        }
+        b->kernel_ms += r.kernel_ms;
+        ++b->promoted;
+    }
+    return GASTAR_OK;
+}
+
 int gastar_batch_rerun(gastar_batch* b) {
     if (!b || !b->uploaded) return GASTAR_BAD_INPUT;
     if (cudaSetDevice(b->ctx->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
@@ -416,10 +512,14 @@ int gastar_batch_rerun(gastar_batch* b) {
         }
         if (!cuda_ok(cudaGraphLaunch(b->graph, st), "cudaGraphLaunch")) return GASTAR_CUDA_ERROR;
     } else {
-        int rc = batch_enqueue(b, st, true);
+        int rc = batch_enqueue(b, st, false);
         if (rc != GASTAR_OK) return rc;
     }
-    return batch_finish(b);
+    int rc = batch_finish(b);
+    if (rc != GASTAR_OK) return rc;
+    rc = batch_retry_overflows(b);
+    if (rc != GASTAR_OK) return rc;
+    return batch_promote(b);
 }
 
 int gastar_batch_result(gastar_batch* b, uint32_t i, gastar_result* out) {
@@ -435,8 +535,11 @@ int gastar_batch_result(gastar_batch* b, uint32_t i, gastar_result* out) {
     out->pushes = c.pushes;
     out->stale = c.stale;
     out->table_used = c.table_used;
-    out->kernel_ms = b->kernel_ms;
+    // Per-instance device time from its first iteration to its last.
+    out->kernel_ms = c.t_end > c.t_start ? (float)((double)(c.t_end - c.t_start) * 1e-6) : 0.f;
+    out->total_ms = b->kernel_ms;
     out->attempts = 1;
+    out->launches = 2;
     return GASTAR_OK;
 }
 
@@ -446,7 +549,7 @@ int gastar_batch_path(gastar_batch* b, uint32_t i, void* path, uint32_t cap, uin
     if (len) *len = c.status == ST_OK ? c.path_len : 0;
     if (c.status != ST_OK) return GASTAR_OK;
     if (c.path_len > cap) return GASTAR_PATH_CAP;
-    const BatchInst& in = b->insts[i];
+    const Problem& in = b->insts[i];
     const uint32_t kw = key_words(in.kind);
     if (c.path_off + (uint64_t)c.path_len * kw > b->h_paths.size()) return GASTAR_PATH_CAP;
     const unsigned long long* src = b->h_paths.data() + c.path_off;

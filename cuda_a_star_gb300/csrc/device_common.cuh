@@ -199,22 +199,42 @@ __device__ __forceinline__ Entry<KW> pick(const Entry<KW>& lo, const Entry<KW>& 
 // order is node-wise (every entry of a node <= every entry of its children),
 // so the root holds the 32 best entries of the tree.  The root node and a
 // partial buffer of < 32 entries live in registers (one entry per lane) for
-// the lifetime of a launch; the other nodes are 512-byte (or 1 KiB) blocks in
-// global memory, read and written with one coalesced access per lane.
-// Replaces the reference's one-thread-per-heap binary heaps with their
-// key->slot index (heaps.h:93-177, device_hashmap.h): stale entries are
-// dropped at pop time instead of being erased (lazy deletion).
+// the lifetime of a launch, nodes 1..kHeapSmemNodes-1 in shared memory, the
+// rest are 512-byte (or 1 KiB) blocks in global memory read and written with
+// one coalesced access per lane.  Replaces the reference's one-thread-per-heap
+// binary heaps with their key->slot index (heaps.h:93-177, device_hashmap.h):
+// stale entries are dropped at pop time instead of being erased (lazy
+// deletion).
 // ---------------------------------------------------------------------------
+constexpr uint32_t kHeapSmemNodes = 7;  // nodes 1..6 staged in shared memory
+
 template <int KW> struct WarpHeap {
-    Entry<KW>* nodes;  // (cap + 1) * 32 entries; node `cap` stores the saved partial buffer
-    uint32_t* hdr;     // saved {N, pc}
-    uint32_t cap;      // tree nodes available
-    uint32_t N;        // full nodes in the tree (warp-uniform)
-    uint32_t pc;       // entries in the partial buffer (warp-uniform)
-    uint32_t max_n;    // high-water mark of N
-    Entry<KW> root;    // lane l: root[l] (valid iff N > 0)
-    Entry<KW> part;    // lane l: partial[l] (valid iff l < pc), ascending
+    Entry<KW>* nodes;   // (cap + 1) * 32 entries; node `cap` stores the saved partial buffer
+    Entry<KW>* snodes;  // shared memory: nodes 1..kHeapSmemNodes-1
+    uint32_t* hdr;      // saved {N, pc}
+    uint32_t cap;       // tree nodes available (>= kHeapSmemNodes)
+    uint32_t N;         // full nodes in the tree (warp-uniform)
+    uint32_t pc;        // entries in the partial buffer (warp-uniform)
+    uint32_t max_n;     // high-water mark of N
+    Entry<KW> root;     // lane l: root[l] (valid iff N > 0)
+    Entry<KW> part;     // lane l: partial[l] (valid iff l < pc), ascending
 };
+
+template <int KW>
+__device__ __forceinline__ Entry<KW> ld_node(const WarpHeap<KW>& h, uint32_t idx, int lane) {
+    if (idx < kHeapSmemNodes) return ld_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, false);
+    return ld_entry(h.nodes + (size_t)idx * 32 + lane);
+}
+template <int KW>
+__device__ __forceinline__ void st_node(const WarpHeap<KW>& h, uint32_t idx, int lane, const Entry<KW>& e) {
+    if (idx < kHeapSmemNodes) st_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, e, false);
+    else st_entry(h.nodes + (size_t)idx * 32 + lane, e);
+}
+// Priority of the largest entry of node idx (one read, broadcast to the warp).
+template <int KW> __device__ __forceinline__ uint64_t node_max(const WarpHeap<KW>& h, uint32_t idx) {
+    if (idx < kHeapSmemNodes) return *reinterpret_cast<const volatile uint64_t*>(&h.snodes[(size_t)(idx - 1) * 32 + 31].prio);
+    return __ldcg(reinterpret_cast<const unsigned long long*>(&h.nodes[(size_t)idx * 32 + 31].prio));
+}
 
 template <int KW> __device__ __forceinline__ void heap_init(WarpHeap<KW>& h) {
     h.N = 0;
@@ -230,10 +250,16 @@ template <int KW> __device__ __forceinline__ void heap_restore(WarpHeap<KW>& h, 
     h.max_n = h.N;
     h.root = h.N ? ld_entry(h.nodes + lane) : inf_entry<KW>();
     h.part = (uint32_t)lane < h.pc ? ld_entry(h.nodes + (size_t)h.cap * 32 + lane) : inf_entry<KW>();
+    for (uint32_t i = 1; i < h.N && i < kHeapSmemNodes; ++i)
+        st_stage(h.snodes + (size_t)(i - 1) * 32 + lane, ld_entry(h.nodes + (size_t)i * 32 + lane), false);
+    __syncwarp();
 }
 
 template <int KW> __device__ __forceinline__ void heap_save(const WarpHeap<KW>& h, int lane) {
+    __syncwarp();
     if (h.N) st_entry(h.nodes + lane, h.root);
+    for (uint32_t i = 1; i < h.N && i < kHeapSmemNodes; ++i)
+        st_entry(h.nodes + (size_t)i * 32 + lane, ld_stage(h.snodes + (size_t)(i - 1) * 32 + lane, false));
     st_entry(h.nodes + (size_t)h.cap * 32 + lane, h.part);
     if (lane == 0) {
         __stcg(h.hdr, h.N);
@@ -256,19 +282,19 @@ template <int KW> __device__ void heap_sift_down(WarpHeap<KW>& h, int lane) {
     for (;;) {
         uint32_t l = 2 * idx + 1, r = l + 1;
         if (l >= h.N) break;
-        Entry<KW> L = ld_entry(h.nodes + (size_t)l * 32 + lane);
+        Entry<KW> L = ld_node(h, l, lane);
         uint64_t cmax = __shfl_sync(kFull, cur.prio, 31);
         uint64_t lmin = __shfl_sync(kFull, L.prio, 0);
         if (r >= h.N) {
             if (cmax > lmin) {
                 Entry<KW> lo, hi;
                 merge2(cur, L, lo, hi, lane);
-                st_entry(h.nodes + (size_t)l * 32 + lane, hi);
+                st_node(h, l, lane, hi);
                 cur = lo;
             }
             break;
         }
-        Entry<KW> R = ld_entry(h.nodes + (size_t)r * 32 + lane);
+        Entry<KW> R = ld_node(h, r, lane);
         uint64_t rmin = __shfl_sync(kFull, R.prio, 0);
         if (cmax <= (lmin < rmin ? lmin : rmin)) break;
         uint64_t lmax = __shfl_sync(kFull, L.prio, 31);
@@ -276,16 +302,17 @@ template <int KW> __device__ void heap_sift_down(WarpHeap<KW>& h, int lane) {
         Entry<KW> A, B;
         merge2(L, R, A, B, lane);
         uint32_t big = lmax >= rmax ? l : r, small = big == l ? r : l;
-        st_entry(h.nodes + (size_t)big * 32 + lane, B);  // B.max = max(lmax, rmax): big's subtree stays ordered
+        st_node(h, big, lane, B);  // B.max = max(lmax, rmax): big's subtree stays ordered
         Entry<KW> lo, hi;
         merge2(cur, A, lo, hi, lane);
         if (idx == 0) h.root = lo;
-        else st_entry(h.nodes + (size_t)idx * 32 + lane, lo);
+        else st_node(h, idx, lane, lo);
         cur = hi;
         idx = small;
     }
     if (idx == 0) h.root = cur;
-    else st_entry(h.nodes + (size_t)idx * 32 + lane, cur);
+    else st_node(h, idx, lane, cur);
+    __syncwarp();
 }
 
 // Pops up to E (1..32) best entries whose priority is below `lim`; lane
@@ -329,7 +356,7 @@ __device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, uint64_t lim, Entry<KW
         h.part = r1;
         h.pc = rest;
     } else {
-        Entry<KW> last = ld_entry(h.nodes + (size_t)(h.N - 1) * 32 + lane);
+        Entry<KW> last = ld_node(h, h.N - 1, lane);
         h.N -= 1;
         Entry<KW> lo2, hi2;
         merge2(last, r1, lo2, hi2, lane);
@@ -363,19 +390,24 @@ template <int KW> __device__ bool heap_insert_node(WarpHeap<KW>& h, Entry<KW> F,
             F = hi;
         }
     }
+    // The path is fixed by the new leaf's index: fetch the maximum of every
+    // node on it in one parallel load (lane j <- depth j), so only the nodes
+    // that need a merge cost a dependent access.
+    uint64_t pmax = kInfPrio;
+    if (lane >= 1 && lane < levels) pmax = node_max(h, (p >> (levels - lane)) - 1);
     for (int b = levels - 1; b >= 1; --b) {
-        Entry<KW>* np = h.nodes + (size_t)((p >> b) - 1) * 32;
+        const uint32_t idx = (p >> b) - 1;
         uint64_t fmin = __shfl_sync(kFull, F.prio, 0);
-        uint64_t mmax = __ldcg(reinterpret_cast<const unsigned long long*>(&np[31].prio));
-        if (fmin < mmax) {
-            Entry<KW> M = ld_entry(np + lane);
+        if (fmin < __shfl_sync(kFull, pmax, levels - b)) {
+            Entry<KW> M = ld_node(h, idx, lane);
             Entry<KW> lo, hi;
             merge2(M, F, lo, hi, lane);
-            st_entry(np + lane, lo);
+            st_node(h, idx, lane, lo);
             F = hi;
         }
     }
-    st_entry(h.nodes + (size_t)h.N * 32 + lane, F);
+    st_node(h, h.N, lane, F);
+    __syncwarp();
     h.N += 1;
     if (h.N > h.max_n) h.max_n = h.N;
     return true;
@@ -516,5 +548,67 @@ __device__ __forceinline__ uint64_t tab_get(const HashTab128& t, uint64_t k0, ui
 struct DenseTab {
     unsigned long long* v;
 };
+
+// Two-step insert-or-min used by the expansion loop, so that the probes of all
+// successors of a lane are in flight together: claim_first issues one CAS at
+// the home slot (1 = claimed, 0 = found, 2 = occupied by another key),
+// claim_probe walks on from there (-1 = full), min_at applies the atomicMin
+// to the value word and returns the old value.
+__device__ __forceinline__ int tab_claim_first(const HashTab64& t, uint64_t key, uint64_t& slot) {
+    const uint64_t i = mix64(key) & t.mask;
+    slot = 2 * i;
+    const unsigned long long k = atomicCAS(t.s + 2 * i, kEmpty, key);
+    return k == kEmpty ? 1 : (k == key ? 0 : 2);
+}
+__device__ __forceinline__ int tab_claim_probe(const HashTab64& t, uint64_t key, uint64_t& slot) {
+    uint64_t i = slot / 2;
+    for (uint32_t p = 1; p < t.max_probe; ++p) {
+        i = (i + 1) & t.mask;
+        unsigned long long* ks = t.s + 2 * i;
+        unsigned long long k = __ldcg(ks);
+        int claimed = 0;
+        if (k == kEmpty) {
+            k = atomicCAS(ks, kEmpty, key);
+            if (k == kEmpty) {
+                k = key;
+                claimed = 1;
+            }
+        }
+        if (k == key) {
+            slot = 2 * i;
+            return claimed;
+        }
+    }
+    return -1;
+}
+__device__ __forceinline__ uint64_t tab_min_at(const HashTab64& t, uint64_t slot, uint64_t val) {
+    return atomicMin(t.s + slot + 1, val);
+}
+
+__device__ __forceinline__ int tab_claim_first(const HashTab128& t, uint64_t k0, uint64_t k1, uint64_t& slot) {
+    const uint64_t i = hash128(k0, k1) & t.mask;
+    slot = 4 * i;
+    uint64_t o0, o1;
+    cas128(t.s + 4 * i, kEmpty, kEmpty, k0, k1, o0, o1);
+    if (o0 == kEmpty && o1 == kEmpty) return 1;
+    return (o0 == k0 && o1 == k1) ? 0 : 2;
+}
+__device__ __forceinline__ int tab_claim_probe(const HashTab128& t, uint64_t k0, uint64_t k1, uint64_t& slot) {
+    uint64_t i = slot / 4;
+    for (uint32_t p = 1; p < t.max_probe; ++p) {
+        i = (i + 1) & t.mask;
+        uint64_t o0, o1;
+        cas128(t.s + 4 * i, kEmpty, kEmpty, k0, k1, o0, o1);
+        const int claimed = (o0 == kEmpty && o1 == kEmpty);
+        if (claimed || (o0 == k0 && o1 == k1)) {
+            slot = 4 * i;
+            return claimed;
+        }
+    }
+    return -1;
+}
+__device__ __forceinline__ uint64_t tab_min_at(const HashTab128& t, uint64_t slot, uint64_t val) {
+    return atomicMin(t.s + slot + 2, val);
+}
 
 }  // namespace gastar

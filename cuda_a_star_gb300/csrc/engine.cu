@@ -73,11 +73,14 @@ uint32_t entry_bytes(uint32_t kind) { return kind == KIND_SLIDING5 ? 32u : 16u; 
 uint32_t max_neighbours(uint32_t kind) { return kind == KIND_GRID ? 8u : 4u; }
 uint32_t key_words(uint32_t kind) { return kind == KIND_SLIDING5 ? 2u : 1u; }
 
-size_t stage_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew) {
+size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi) {
+    // Two stage buffers (one-block teams) + shared-memory heap nodes per warp.
     size_t best = 0;
     for (uint32_t k = 0; k < 4; ++k)
-        if (kinds & kind_bit(k))
-            best = std::max(best, (size_t)warps * ew * max_neighbours(k) * entry_bytes(k));
+        if (kinds & kind_bit(k)) {
+            const size_t stage = multi ? 0 : 2 * stage_entries_per_buffer(warps, ew, max_neighbours(k)) * entry_bytes(k);
+            best = std::max(best, stage + (size_t)warps * (kHeapSmemNodes - 1) * 32 * entry_bytes(k));
+        }
     return best;
 }
 
@@ -101,11 +104,19 @@ int launch_search(gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t
         GA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     LaunchParams p = P;
     void* args[] = {&p};
-    if (P.team_ctas > 1) {
-        GA_CUDA(cudaLaunchCooperativeKernel(f, dim3(blocks), dim3(threads), args, smem, st));
-    } else {
-        GA_CUDA(cudaLaunchKernel(f, dim3(blocks), dim3(threads), args, smem, st));
-    }
+    // Blocks that wait on each other (multi-block teams) need a cooperative
+    // launch, which guarantees they are resident together.
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(blocks);
+    lc.blockDim = dim3(threads);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = (P.team_ctas > 1 || P.n_heavy > 0) ? 1 : 0;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    GA_CUDA(cudaLaunchKernelExC(&lc, f, args));
     return GASTAR_OK;
 }
 
@@ -292,13 +303,6 @@ int gastar_device_info(gastar_ctx* c, int* sm_count, uint64_t* mem_bytes, char* 
 // ---------------------------------------------------------------------------
 namespace gastar {
 
-struct PlainProblem {
-    uint32_t kind, n;
-    uint64_t start0, start1, goal0, goal1;
-    const uint8_t* d_weights;  // grid (device)
-    uint32_t W, H, minw, f0;
-};
-
 static void fill_result(gastar_result* out, const InstCtl& c) {
     out->status = (int32_t)c.status;
     out->cost = c.status == ST_OK || c.status == ST_PATH_CAP ? c.best : 0;
@@ -329,7 +333,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     uint64_t heaps = (Q + ew - 1) / ew;
     uint64_t blocks = (heaps + W - 1) / W;
     const bool multi = blocks > 1;
-    const size_t smem = multi ? 0 : stage_smem_bytes(kinds, W, ew);
+    const size_t smem = block_smem_bytes(kinds, W, ew, multi);
     const int nb = occupancy_blocks(c, kinds, threads, smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
     uint64_t max_blocks = (uint64_t)nb * c->sms;
@@ -362,10 +366,17 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         limit = (uint64_t)((double)slots * lf);
         touched_cap = limit + heaps * ew * maxn + 16;
         tb = &c->table;
-        if (!tb->ensure(table_words * 8) || !c->touched.ensure(touched_cap * 4) || !c->misc.ensure(64))
-            return GASTAR_OUT_OF_MEMORY;
+        // A reallocated table, claim list or claim counter loses the record of
+        // what the previous solve wrote: clear the whole table then.
+        bool lost = false;
+        if (!tb->ensure(table_words * 8)) return GASTAR_OUT_OF_MEMORY;
+        lost |= tb->fresh;
+        if (!c->touched.ensure(touched_cap * 4)) return GASTAR_OUT_OF_MEMORY;
+        lost |= c->touched.fresh;
+        if (!c->misc.ensure(64)) return GASTAR_OUT_OF_MEMORY;
+        lost |= c->misc.fresh;
         touched_cap = c->touched.n / 4;
-        if (tb->fresh || c->table_dirty) {
+        if (lost || c->table_dirty) {
             GA_CUDA(cudaMemsetAsync(tb->p, 0xff, tb->n, st));
             GA_CUDA(cudaMemsetAsync(c->misc.p, 0, 8, st));  // claim-list length
             c->table_dirty = false;
@@ -373,10 +384,10 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     }
     // Heaps: per warp-heap node capacity with headroom for uneven dealing.
     uint64_t per_heap = (heap_entries + heaps - 1) / heaps;
-    uint64_t cap_nodes = std::max<uint64_t>(4, (per_heap * 2 + 31) / 32);
+    uint64_t cap_nodes = std::max<uint64_t>(2 * kHeapSmemNodes, (per_heap * 2 + 31) / 32);
     if (cap_nodes > 0x7fffffffull) return GASTAR_OUT_OF_MEMORY;
     const size_t heap_bytes = (size_t)heaps * (cap_nodes + 1) * 32 * ebytes;
-    const size_t stage_entries = multi ? (size_t)heaps * ew * maxn : 0;
+    const size_t stage_entries = multi ? 2 * stage_entries_per_buffer(heaps, ew, maxn) : 0;
 
     if (!c->heaps.ensure(heap_bytes) || !c->hdr.ensure((size_t)heaps * 8) ||
         !c->stage.ensure(std::max<size_t>(stage_entries * ebytes, 16)) ||
@@ -426,6 +437,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     std::memset(&tc, 0, sizeof(tc));
     for (auto& s : tc.slot) {
         s.minprio = ~0ull;
+        s.minstage = ~0ull;
         s.best = kInf;
     }
     c->h_team = tc;

@@ -27,7 +27,7 @@ const void* search_kernel_for(uint32_t kinds);
 uint32_t entry_bytes(uint32_t kind);
 uint32_t max_neighbours(uint32_t kind);
 uint32_t key_words(uint32_t kind);
-size_t stage_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew);
+size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi);
 int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st);
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
@@ -35,6 +35,17 @@ int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
 int occupancy_blocks(struct ::gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem);
 int device_min_weight(struct ::gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStream_t st,
                       uint32_t* out);
+
+struct PlainProblem {
+    uint32_t kind, n;
+    uint64_t start0, start1, goal0, goal1;
+    const uint8_t* d_weights;  // grid (device)
+    uint32_t W, H, minw, f0;
+};
+// One instance on a multi-block team (the plain engine); path_keys receives
+// the path goal-first (KW words per state) when not null.
+int plain_solve(struct ::gastar_ctx* c, const PlainProblem& pp, const gastar_config* user_cfg,
+                std::vector<uint64_t>* path_keys, gastar_result* out);
 
 bool valid_board(uint32_t n, const uint8_t* b);
 void pack_board(uint32_t n, const uint8_t* b, uint64_t& lo, uint64_t& hi);

@@ -3,12 +3,25 @@
 
 #include <cstdint>
 
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#endif
+
 namespace gastar {
 
 // Problem kinds compiled into the search kernel.
 enum Kind : uint32_t { KIND_SLIDING3 = 0, KIND_SLIDING4 = 1, KIND_SLIDING5 = 2, KIND_GRID = 3 };
 constexpr uint32_t kKindsAll = 0xf;
 constexpr uint32_t kind_bit(uint32_t k) { return 1u << k; }
+
+// Entries one stage buffer must hold: every popped entry of every warp-heap
+// can stage all of its successors.  Dynamic shared memory of one block holds
+// two stage buffers (one-block teams only) followed by the shared-memory heap
+// nodes of every warp.
+inline __host__ __device__ size_t stage_entries_per_buffer(uint32_t heaps, uint32_t ew, uint32_t maxn) {
+    return (size_t)heaps * ew * maxn;
+}
 
 // Per-instance control block, written by the device.
 struct alignas(16) InstCtl {
@@ -21,7 +34,7 @@ struct alignas(16) InstCtl {
     uint64_t t_start;     // device globaltimer at the first iteration
     unsigned long long expansions, generated, pushes, stale, table_used;
     unsigned long long path_off;  // offset (64-bit words) of the path in the path arena
-    unsigned long long pad;
+    uint64_t t_end;               // device globaltimer when the search finished
 };
 
 // Per-instance description, written by the host.
@@ -51,18 +64,21 @@ struct alignas(16) InstDesc {
     uint32_t prev_slot_words, pad1;
 };
 
+// Per-iteration team state; iteration t uses slot t % kSlots.
 struct alignas(16) TeamSlot {
-    unsigned long long minprio;  // min priority over the team's heaps after the push phase
-    uint32_t count;              // entries staged in the pop/expand phase
-    uint32_t best;               // goal costs found in the pop/expand phase
-    uint32_t err;                // first error raised in the iteration
-    uint32_t pad[3];
+    unsigned long long minprio;   // min priority over the team's heaps after the push phase
+    unsigned long long minstage;  // min priority of the entries staged in the pop/expand phase
+    uint32_t count;               // entries staged in the pop/expand phase
+    uint32_t best;                // goal costs found in the pop/expand phase
+    uint32_t err;                 // first error raised in the iteration
+    uint32_t pad;
 };
+constexpr uint32_t kSlots = 4;
 
 // Control of a multi-block team (one instance on many blocks).
 struct alignas(16) TeamCtl {
-    uint32_t arrive, gen, abort, pad;
-    TeamSlot slot[3];
+    uint32_t arrive, gen, abort, inst;  // barrier state; instance the team works on
+    TeamSlot slot[kSlots];
 };
 
 struct LaunchParams {
@@ -76,6 +92,16 @@ struct LaunchParams {
     TeamCtl* team;            // multi-block team control (device)
     void* stage;              // multi-block stage buffer (device)
     uint64_t barrier_timeout_ns;
+    // Heavy instances of a batch: blocks [0, heavy_teams * heavy_team) first
+    // work in teams of heavy_team blocks on heavy_order[0..n_heavy), then join
+    // the one-block loop.  Each team owns heavy_ctl[t] and a stage area of
+    // heavy_stage_bytes at heavy_stage + t * heavy_stage_bytes.
+    const uint32_t* heavy_order;
+    uint32_t n_heavy, heavy_team, heavy_teams, pad1;
+    uint32_t* heavy_next;
+    TeamCtl* heavy_ctl;
+    void* heavy_stage;
+    uint64_t heavy_stage_bytes;
 };
 
 }  // namespace gastar

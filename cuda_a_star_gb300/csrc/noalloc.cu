@@ -35,7 +35,7 @@ using namespace gastar;
 
 constexpr uint32_t kWarps = 4;           // warp-heaps of the single block
 constexpr uint32_t kEw = 32;             // pops per warp-heap per iteration
-constexpr uint64_t kSlots = 1ull << 19;  // hash slots: 181,440 states at load 0.35
+constexpr uint64_t kTableSlots = 1ull << 19;  // hash slots: 181,440 states at load 0.35
 constexpr uint32_t kHeapCap = 4095;      // nodes per warp-heap (131,040 entries)
 constexpr uint64_t kPathWords = 4096;    // path arena (states)
 
@@ -46,7 +46,7 @@ constexpr size_t kUsedOff = 648;         // u64 path-arena fill
 constexpr size_t kHdrOff = 1024;         // kWarps x {N, pc}
 constexpr size_t kPathOff = 4096;
 constexpr size_t kTableOff = kPathOff + kPathWords * 8;
-constexpr size_t kHeapOff = kTableOff + kSlots * 16;
+constexpr size_t kHeapOff = kTableOff + kTableSlots * 16;
 constexpr size_t kScratchBytes = kHeapOff + (size_t)kWarps * (kHeapCap + 1) * 32 * 16;
 
 static_assert(sizeof(InstDesc) <= kCtlOff - kDescOff, "descriptor does not fit");
@@ -128,9 +128,9 @@ extern "C" int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t* start, co
     pack_board(3, goal, d.goal0, d.goal1);
     d.f0 = sliding_h(3, start, goal, cf.heuristic);
     d.table = reinterpret_cast<unsigned long long*>(b + kTableOff);
-    d.table_words = kSlots * 2;
-    d.table_mask = kSlots - 1;
-    d.table_limit = kSlots - kSlots / 8;
+    d.table_words = kTableSlots * 2;
+    d.table_mask = kTableSlots - 1;
+    d.table_limit = kTableSlots - kTableSlots / 8;
     d.max_probe = 4096;
     d.heaps = kWarps;
     d.heap_nodes = b + kHeapOff;
@@ -167,7 +167,7 @@ extern "C" int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t* start, co
     out->h2d_bytes = sizeof(d);
     const void* kern = reinterpret_cast<const void*>(&search_kernel<kind_bit(KIND_SLIDING3)>);
     void* args[] = {&P};
-    const size_t smem = (size_t)kWarps * kEw * 4 * 16;
+    const size_t smem = 2 * stage_entries_per_buffer(kWarps, kEw, 4) * 16 + (size_t)kWarps * (kHeapSmemNodes - 1) * 32 * 16;
     if ((e = cudaLaunchKernel(kern, dim3(1), dim3(kWarps * 32), args, smem, st)) != cudaSuccess)
         return fail(e, "cudaLaunchKernel");
     out->launches = 1;

@@ -1,0 +1,52 @@
+// Host-side problem records and per-instance partition planning shared by the
+// batched and the served engines.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "engine_types.h"
+
+namespace gastar {
+
+// One instance as the host keeps it.
+struct Problem {
+    uint32_t kind = 0, n = 0;
+    uint64_t start0 = 0, start1 = 0, goal0 = 0, goal1 = 0;
+    uint32_t W = 0, H = 0, minw = 0, f0 = 0;
+    bool unreachable = false;      // other parity class of the standard sliding moves
+    std::vector<uint8_t> weights;  // grid
+    uint64_t est = 0;              // scheduling estimate (larger first)
+};
+
+// Sizing knobs of a partition.
+struct PartConfig {
+    uint32_t warps = 8, ew = 32;
+    float load_factor = 0.75f;
+    uint32_t heuristic = 0, moves = 0, delta_grid = 0;
+    uint64_t sliding_states = 0;  // 0 = by class
+    uint64_t max_exp = 0;
+    uint32_t timeout_ms = 0;
+    uint32_t retry_level = 0;     // capacities scale by 4^retry_level
+    bool own_weights = false;     // grid weights live inside the partition
+};
+
+// Byte layout of one partition: table | heap headers | heap nodes | weights.
+struct PartPlan {
+    uint64_t table_words = 0, table_mask = 0, table_limit = 0;
+    uint32_t heap_cap = 0;
+    uint64_t heap_off = 0, weights_off = 0, bytes = 0;
+    uint64_t path_words = 0;      // path-arena share
+};
+
+bool make_sliding_problem(uint32_t n, const uint8_t* start, const uint8_t* goal, uint32_t heuristic,
+                          uint32_t moves, Problem& p);
+bool make_grid_problem(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx, uint32_t sy,
+                       uint32_t tx, uint32_t ty, uint32_t heuristic, Problem& p);
+PartPlan plan_partition(const Problem& p, const PartConfig& c);
+// Fills an instance descriptor for a partition placed at `base` (256-byte
+// aligned).  `d_weights` is used for grids unless the partition owns them.
+void fill_desc(InstDesc& d, const Problem& p, const PartConfig& c, const PartPlan& plan, char* base,
+               const uint8_t* d_weights, InstCtl* ctl);
+
+}  // namespace gastar

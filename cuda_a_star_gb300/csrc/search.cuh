@@ -117,6 +117,18 @@ template <int N> struct SlidingDom {
         if constexpr (KW == 1) return tab_insert(t, k, v, old, slot);
         else return tab_insert(t, uint64_t(k), uint64_t(k >> 64), v, old, slot);
     }
+    static constexpr bool kDense = false;
+    static __device__ __forceinline__ int claim_first(const Tab& t, KeyT k, uint64_t& slot) {
+        if constexpr (KW == 1) return tab_claim_first(t, k, slot);
+        else return tab_claim_first(t, uint64_t(k), uint64_t(k >> 64), slot);
+    }
+    static __device__ __forceinline__ int claim_probe(const Tab& t, KeyT k, uint64_t& slot) {
+        if constexpr (KW == 1) return tab_claim_probe(t, k, slot);
+        else return tab_claim_probe(t, uint64_t(k), uint64_t(k >> 64), slot);
+    }
+    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, uint64_t v) {
+        return tab_min_at(t, slot, v);
+    }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
     static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
     static __device__ __forceinline__ Pre prepare(const Ctx&, KeyT k) { return blank_of(k); }
@@ -204,6 +216,15 @@ struct GridDom {
         slot = k;
         return old == kEmpty ? 1 : 0;
     }
+    static constexpr bool kDense = true;
+    static __device__ __forceinline__ int claim_first(const Tab&, KeyT k, uint64_t& slot) {
+        slot = k;
+        return 0;
+    }
+    static __device__ __forceinline__ int claim_probe(const Tab&, KeyT, uint64_t&) { return -1; }
+    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, uint64_t v) {
+        return atomicMin(t.v + slot, v);
+    }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
     static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
     static __device__ __forceinline__ Pre prepare(const Ctx& c, KeyT k) {
@@ -241,9 +262,9 @@ struct GridDom {
 // Block-shared state.
 // ---------------------------------------------------------------------------
 struct CtaShared {
-    TeamSlot slot[3];  // team slots of a one-block team
+    TeamSlot slot[kSlots];  // team slots of a one-block team
     InstDesc desc;
-    uint32_t inst, run_best, ok, pad;
+    uint32_t inst, ok, pad0, pad1;
     union {
         SlidingDom<3>::Ctx s3;
         SlidingDom<4>::Ctx s4;
@@ -296,18 +317,49 @@ __device__ __forceinline__ uint64_t ld_vol64(const unsigned long long* p) {
     return *(const volatile unsigned long long*)p;
 }
 
+// The blocks working on one instance.
+struct TeamRef {
+    uint32_t ctas;  // blocks in the team (1 = one block, barriers are __syncthreads)
+    uint32_t rank;  // this block's rank in the team
+    TeamCtl* ctl;   // control block of a multi-block team (device)
+    void* stage;    // stage buffers of a multi-block team (device)
+};
+
+// Inclusive warp prefix sum.
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_min64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t t = __shfl_xor_sync(kFull, v, o);
+        v = t < v ? t : v;
+    }
+    return v;
+}
+
+
 template <class D>
-__device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared& sm,
-                             typename D::Ctx& ctx) {
+__device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared& sm,
+                                          typename D::Ctx& ctx, const TeamRef tm) {
     constexpr int KW = D::KW;
+    constexpr int MAXN = D::MAXN;
     using E = Entry<KW>;
     using KeyT = typename D::KeyT;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const bool multi = P.team_ctas > 1;
-    const uint32_t rank = multi ? blockIdx.x : 0;
+    const bool multi = tm.ctas > 1;
+    const uint32_t rank = tm.rank;
     const uint32_t H = d.heaps;
-    TeamSlot* slots = multi ? P.team->slot : sm.slot;
-    E* stage = multi ? reinterpret_cast<E*>(P.stage) : reinterpret_cast<E*>(g_dyn_smem);
+    TeamSlot* slots = multi ? tm.ctl->slot : sm.slot;
+    const size_t stage_cap = stage_entries_per_buffer(H, d.ew, MAXN);
+    char* dyn = reinterpret_cast<char*>(g_dyn_smem);
+    E* const stage0 = multi ? reinterpret_cast<E*>(tm.stage) : reinterpret_cast<E*>(dyn);
+    E* const snodes_all = reinterpret_cast<E*>(dyn + (multi ? 0 : 2 * stage_cap * sizeof(E)));
     InstCtl* ctl = d.ctl;
     const bool leader = rank == 0 && threadIdx.x == 0;
 
@@ -316,7 +368,7 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
             __syncthreads();
             return true;
         }
-        return team_sync_grid(P.team, P.team_ctas, P.barrier_timeout_ns, sm);
+        return team_sync_grid(tm.ctl, tm.ctas, P.barrier_timeout_ns, sm);
     };
 
     D::load(ctx, d);
@@ -325,22 +377,27 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
     WarpHeap<KW> hp;
     const uint32_t hid = rank * W + warp;
     hp.nodes = reinterpret_cast<E*>(d.heap_nodes) + (size_t)hid * (d.heap_cap + 1) * 32;
+    hp.snodes = snodes_all + (size_t)warp * (kHeapSmemNodes - 1) * 32;
     hp.hdr = d.heap_hdr + 2 * hid;
     hp.cap = d.heap_cap;
 
     const uint32_t life = ld_vol(&ctl->life);
-    if (!multi && threadIdx.x < 3) {
-        sm.slot[threadIdx.x].minprio = kInfPrio;
-        sm.slot[threadIdx.x].count = 0;
-        sm.slot[threadIdx.x].best = kInf;
-        sm.slot[threadIdx.x].err = 0;
+    if (!multi && threadIdx.x < kSlots) {
+        TeamSlot& t = sm.slot[threadIdx.x];
+        t.minprio = kInfPrio;
+        t.minstage = kInfPrio;
+        t.count = 0;
+        t.best = kInf;
+        t.err = 0;
     }
     uint32_t status = kInf;  // kInf while running / suspended
+    uint32_t best_r;         // best goal cost seen (identical in every thread)
+    bool have_prev;          // the previous iteration's slot holds the heaps' min
     if (life == LIFE_FRESH) {
         // Clear the table (0xff = empty key and value) across the whole team:
         // only the slots the previous solve claimed when they were recorded,
         // otherwise the whole table.
-        const uint64_t stride = (uint64_t)P.team_ctas * blockDim.x;
+        const uint64_t stride = (uint64_t)tm.ctas * blockDim.x;
         const uint64_t tid = (uint64_t)rank * blockDim.x + threadIdx.x;
         if (d.touched) {
             const uint64_t cnt = ld_vol64(d.touched_count);
@@ -374,35 +431,54 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
             atomicAdd(&ctl->table_used, 1ull);
             ctl->t_start = globaltimer_ns();
         }
-        if (threadIdx.x == 0) sm.run_best = D::is_goal(ctx, ctx.start) ? 0u : kInf;
+        best_r = D::is_goal(ctx, ctx.start) ? 0u : kInf;
+        have_prev = true;  // the start is the only open entry; every slot starts empty
     } else {
         heap_restore(hp, lane);
-        if (threadIdx.x == 0) sm.run_best = ld_vol(&ctl->best);
+        best_r = ld_vol(&ctl->best);
+        have_prev = false;
     }
     if (status == kInf && !tsync()) status = ST_BARRIER;
 
     const uint32_t ew = d.ew;
-    uint32_t fmin = d.f0;  // min f over the open list after the previous iteration
+    uint32_t fmin = d.f0;  // min f over the open list at the last check
     uint32_t it = 0;
     const uint32_t it0 = ld_vol(&ctl->iterations);
     while (status == kInf) {
-        const uint32_t s = it % 3;
+        const uint32_t s = it % kSlots;
         TeamSlot* S = slots + s;
-        const uint32_t rb = sm.run_best;
+        E* const stage = stage0 + (size_t)(it & 1) * stage_cap;
+        if (leader) {
+            // Slot it+1 was last read right after the barrier of iteration
+            // it-2; every block is past that point, and none writes it before
+            // the barrier of this iteration.
+            TeamSlot* nx = slots + (it + 1) % kSlots;
+            nx->minprio = kInfPrio;
+            nx->minstage = kInfPrio;
+            nx->count = 0;
+            nx->best = kInf;
+            nx->err = 0;
+            if (ld_vol64(&ctl->table_used) > d.table_limit) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+            if (d.max_exp && ld_vol64(&ctl->expansions) >= d.max_exp) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
+            if (d.max_iter && it0 + it + 1 >= d.max_iter) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
+            if (d.timeout_ns && globaltimer_ns() - ctl->t_start > d.timeout_ns)
+                atomicCAS(&S->err, 0u, (uint32_t)ST_TIMEOUT);
+        }
 
-        // ---- pop + expand + insert-or-min ----
-        E e;
-        // Pop window: with delta set, only entries with f <= fmin + delta are
-        // expanded (delta-stepping); the rest wait for later iterations.
+        // ---- pop: up to ew entries per warp-heap, inside the window ----
+        // With delta set, only entries with f <= fmin + delta are expanded
+        // (delta-stepping); the rest wait for later iterations.
         const uint64_t lim = (d.delta && (uint64_t)fmin + d.delta < 0xffffffffull)
                                  ? ((uint64_t)(fmin + d.delta + 1) << 32)
                                  : kInfPrio;
+        E e;
         const uint32_t cnt = heap_pop(hp, ew, lim, e, lane);
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
         uint32_t pm = kRootMove;
         bool stale = false;
+        uint32_t goal_g = kInf;
         if (act) {
             const uint64_t v = D::get(tab, k);
             if ((uint32_t)(v >> 32) < g) {
@@ -413,140 +489,174 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
             }
         }
         if (act && D::is_goal(ctx, k)) {
-            atomicMin(&S->best, g);
+            goal_g = g;
             act = false;
         }
         const unsigned bexp = __ballot_sync(kFull, act), bstale = __ballot_sync(kFull, stale);
+
+        // ---- expand: per group of moves, all successors, then all probes,
+        // then all atomicMins, so each group costs ~2 memory round trips ----
         const typename D::Pre pre = D::prepare(ctx, k);
-        uint32_t n_gen = 0, n_claim = 0, n_push = 0;
+        constexpr int GS = MAXN < 4 ? MAXN : 4;
+        uint32_t n_gen = 0, n_claim = 0, pushed = 0;
+        uint64_t smin = kInfPrio;
         bool tfull = false;
 #pragma unroll
-        for (int m = 0; m < D::MAXN; ++m) {
-            E out = inf_entry<KW>();
-            bool acc = false, claimed = false;
-            uint64_t cslot = 0;
-            if (act) {
-                KeyT nk;
-                uint32_t ng, nh;
-                if (D::succ(ctx, k, pre, m, pm, g, h, nk, ng, nh)) {
-                    ++n_gen;
-                    const uint32_t nf = ng + nh;
-                    if (nf < rb) {
-                        uint64_t old, slot = 0;
-                        const int r = D::insert(tab, nk, make_val(ng, (uint32_t)m), old, slot);
-                        if (r < 0) {
-                            tfull = true;
-                        } else {
-                            n_claim += (uint32_t)r;
-                            claimed = r == 1;
-                            cslot = slot;
-                            if ((uint32_t)(old >> 32) > ng) {
-                                acc = true;
-                                out.prio = make_prio(nf, ng);
-                                D::set_key(out, nk);
-                                if (D::is_goal(ctx, nk)) atomicMin(&S->best, ng);
-                            }
+        for (int g0 = 0; g0 < MAXN; g0 += GS) {
+            KeyT nk[GS];
+            uint32_t ng[GS], nh[GS];
+            bool ok[GS];
+#pragma unroll
+            for (int j = 0; j < GS; ++j) {
+                ok[j] = act && D::succ(ctx, k, pre, g0 + j, pm, g, h, nk[j], ng[j], nh[j]);
+                n_gen += ok[j];
+                ok[j] = ok[j] && ng[j] + nh[j] < best_r;  // cannot beat the best goal found
+            }
+            uint64_t slot[GS];
+            int cl[GS];
+#pragma unroll
+            for (int j = 0; j < GS; ++j) cl[j] = ok[j] ? D::claim_first(tab, nk[j], slot[j]) : -1;
+#pragma unroll
+            for (int j = 0; j < GS; ++j) {
+                if (cl[j] == 2) cl[j] = D::claim_probe(tab, nk[j], slot[j]);
+                if (ok[j] && cl[j] < 0) tfull = true;
+            }
+            uint64_t old[GS];
+#pragma unroll
+            for (int j = 0; j < GS; ++j)
+                old[j] = (ok[j] && cl[j] >= 0) ? D::min_at(tab, slot[j], make_val(ng[j], (uint32_t)(g0 + j)))
+                                               : 0ull;
+            uint32_t nacc = 0, ncl = 0;
+            bool acc[GS], clm[GS];
+#pragma unroll
+            for (int j = 0; j < GS; ++j) {
+                const bool in = ok[j] && cl[j] >= 0;
+                acc[j] = in && (uint32_t)(old[j] >> 32) > ng[j];
+                clm[j] = in && (D::kDense ? old[j] == kEmpty : cl[j] == 1);
+                nacc += acc[j];
+                ncl += clm[j];
+                if (acc[j]) {
+                    const uint64_t pr = make_prio(ng[j] + nh[j], ng[j]);
+                    smin = pr < smin ? pr : smin;
+                    if (D::is_goal(ctx, nk[j]) && ng[j] < goal_g) goal_g = ng[j];
+                }
+            }
+            n_claim += ncl;
+            // Stage the improved successors: one atomic per warp reserves the range.
+            const uint32_t incl = warp_incl_sum(nacc, lane);
+            const uint32_t total = __shfl_sync(kFull, incl, 31);
+            if (total) {
+                uint32_t base = 0;
+                if (lane == 31) base = atomicAdd(&S->count, total);
+                base = __shfl_sync(kFull, base, 31) + incl - nacc;
+#pragma unroll
+                for (int j = 0; j < GS; ++j) {
+                    if (acc[j]) {
+                        E out = inf_entry<KW>();
+                        out.prio = make_prio(ng[j] + nh[j], ng[j]);
+                        D::set_key(out, nk[j]);
+                        st_stage(stage + base++, out, multi);
+                    }
+                }
+                pushed += total;
+            }
+            if (d.touched) {  // record claimed slots for the next solve's clear
+                const uint32_t ci = warp_incl_sum(ncl, lane);
+                const uint32_t ct = __shfl_sync(kFull, ci, 31);
+                if (ct) {
+                    unsigned long long cb = 0;
+                    if (lane == 31) cb = atomicAdd(d.touched_count, (unsigned long long)ct);
+                    cb = __shfl_sync(kFull, cb, 31) + ci - ncl;
+#pragma unroll
+                    for (int j = 0; j < GS; ++j) {
+                        if (clm[j]) {
+                            if (cb < d.touched_cap) d.touched[cb] = (uint32_t)slot[j];
+                            ++cb;
                         }
                     }
                 }
             }
-            if (d.touched) {  // record claimed slots for the next solve's clear
-                const unsigned bc = __ballot_sync(kFull, claimed);
-                if (bc) {
-                    const int ldr = __ffs(bc) - 1;
-                    unsigned long long base = 0;
-                    if (lane == ldr) base = atomicAdd(d.touched_count, (unsigned long long)__popc(bc));
-                    base = __shfl_sync(kFull, base, ldr);
-                    const unsigned long long at = base + __popc(bc & ((1u << lane) - 1u));
-                    if (claimed && at < d.touched_cap) d.touched[at] = (uint32_t)cslot;
-                }
-            }
-            const unsigned bal = __ballot_sync(kFull, acc);
-            if (bal) {
-                const int ldr = __ffs(bal) - 1;
-                uint32_t base = 0;
-                if (lane == ldr) base = atomicAdd(&S->count, (uint32_t)__popc(bal));
-                base = __shfl_sync(kFull, base, ldr);
-                if (acc) st_stage(stage + base + __popc(bal & ((1u << lane) - 1u)), out, multi);
-                n_push += (uint32_t)__popc(bal);
-            }
         }
+        {
+            uint32_t gsum = n_gen, csum = n_claim;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            n_gen += __shfl_xor_sync(kFull, n_gen, o);
-            n_claim += __shfl_xor_sync(kFull, n_claim, o);
-        }
-        const bool any_full = __any_sync(kFull, tfull);
-        if (lane == 0) {
-            if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
-            if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
-            if (n_gen) atomicAdd(&ctl->generated, (unsigned long long)n_gen);
-            if (n_push) atomicAdd(&ctl->pushes, (unsigned long long)n_push);
-            if (n_claim) atomicAdd(&ctl->table_used, (unsigned long long)n_claim);
-            if (any_full) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+            for (int o = 16; o > 0; o >>= 1) {
+                gsum += __shfl_xor_sync(kFull, gsum, o);
+                csum += __shfl_xor_sync(kFull, csum, o);
+                const uint32_t gg = __shfl_xor_sync(kFull, goal_g, o);
+                goal_g = gg < goal_g ? gg : goal_g;
+            }
+            smin = warp_min64(smin);
+            const bool any_full = __any_sync(kFull, tfull);
+            if (lane == 0) {
+                if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
+                if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
+                if (gsum) atomicAdd(&ctl->generated, (unsigned long long)gsum);
+                if (pushed) atomicAdd(&ctl->pushes, (unsigned long long)pushed);
+                if (csum) atomicAdd(&ctl->table_used, (unsigned long long)csum);
+                if (smin != kInfPrio) atomicMin(&S->minstage, (unsigned long long)smin);
+                if (goal_g != kInf) atomicMin(&S->best, goal_g);
+                if (any_full) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+            }
         }
         if (!tsync()) {
             status = ST_BARRIER;
             break;
         }
 
-        // ---- push: deal stage chunks to the warp-heaps ----
-        const uint32_t total = ld_vol(&S->count);
-        const uint32_t nch = (total + 31) / 32;
-        bool hfull = false;
-        for (uint32_t c = (hid + H - it % H) % H; c < nch; c += H) {
-            const uint32_t idx = c * 32 + (uint32_t)lane;
-            E x = idx < total ? ld_stage(stage + idx, multi) : inf_entry<KW>();
-            const uint32_t m = total - c * 32 < 32 ? total - c * 32 : 32;
-            if (!heap_push(hp, x, m, lane)) {
-                hfull = true;
-                break;
+        // ---- termination test (a_star.h:260-262), one iteration behind ----
+        // Open entries now: heaps after the previous push (>= that slot's
+        // min) minus this iteration's pops, plus this iteration's stage.
+        {
+            const uint32_t sb = ld_vol(&S->best);
+            best_r = sb < best_r ? sb : best_r;
+            uint32_t err = ld_vol(&S->err);
+            uint64_t open_min = ld_vol64(&S->minstage);
+            if (have_prev) {
+                const TeamSlot* pv = slots + (it + kSlots - 1) % kSlots;
+                if (!err) err = ld_vol(&pv->err);
+                const uint64_t mp = ld_vol64(&pv->minprio);
+                open_min = mp < open_min ? mp : open_min;
+            }
+            // An iteration that lost entries (full table or heap) proves nothing.
+            if (err == ST_TABLE_FULL || err == ST_HEAP_FULL) status = err;
+            else if (have_prev && best_r != kInf && best_r <= prio_f(open_min)) status = ST_OK;
+            else if (err) status = err;
+            else if (have_prev && open_min == kInfPrio) status = ST_NO_PATH;
+            if (status != kInf) break;
+            if (open_min != kInfPrio) fmin = prio_f(open_min);
+        }
+
+        // ---- push: stage chunks dealt round-robin with a rotating offset ----
+        {
+            const uint32_t total = ld_vol(&S->count);
+            const uint32_t nch = (total + 31) / 32;
+            bool hfull = false;
+            for (uint32_t c = (hid + H - it % H) % H; c < nch; c += H) {
+                const uint32_t idx = c * 32 + (uint32_t)lane;
+                E x = idx < total ? ld_stage(stage + idx, multi) : inf_entry<KW>();
+                const uint32_t m = total - c * 32 < 32 ? total - c * 32 : 32;
+                if (!heap_push(hp, x, m, lane)) {
+                    hfull = true;
+                    break;
+                }
+            }
+            const uint64_t mp = heap_min(hp);
+            if (lane == 0) {
+                atomicMin(&S->minprio, (unsigned long long)mp);
+                if (hfull) atomicCAS(&S->err, 0u, (uint32_t)ST_HEAP_FULL);
             }
         }
-        const uint64_t mp = heap_min(hp);
-        if (lane == 0) {
-            atomicMin(&S->minprio, (unsigned long long)mp);
-            if (hfull) atomicCAS(&S->err, 0u, (uint32_t)ST_HEAP_FULL);
-        }
-        if (threadIdx.x == 0) {
-            const uint32_t sb = ld_vol(&S->best);
-            if (sb < sm.run_best) sm.run_best = sb;
-        }
-        if (leader) {
-            TeamSlot* nx = slots + (s + 1) % 3;
-            nx->minprio = kInfPrio;
-            nx->count = 0;
-            nx->best = kInf;
-            nx->err = 0;
-            if (d.max_exp && ld_vol64(&ctl->expansions) >= d.max_exp) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
-            if (d.max_iter && it0 + it + 1 >= d.max_iter) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
-            if (d.timeout_ns && globaltimer_ns() - ctl->t_start > d.timeout_ns)
-                atomicCAS(&S->err, 0u, (uint32_t)ST_TIMEOUT);
-        }
-        if (!tsync()) {
-            status = ST_BARRIER;
-            break;
-        }
-        const uint32_t err = ld_vol(&S->err);
-        const uint64_t gm = ld_vol64(&S->minprio);
-        const uint32_t best = sm.run_best;
-        fmin = prio_f(gm);
         ++it;
-        // Termination (a_star.h:260-262): best goal cost <= min f of the open list.
-        // An iteration that lost entries (full table or heap) cannot prove optimality.
-        const bool found = best != kInf && best <= prio_f(gm);
-        if (err == ST_TABLE_FULL || err == ST_HEAP_FULL) status = err;
-        else if (found) status = ST_OK;
-        else if (err) status = err;
-        else if (gm == kInfPrio) status = ST_NO_PATH;
-        else if (P.slice_iters && it >= P.slice_iters) break;  // suspend
+        have_prev = true;
+        if (P.slice_iters && it >= P.slice_iters) break;  // suspend
     }
 
     if (lane == 0) atomicMax(&ctl->max_nodes, hp.max_n);
     if (status == kInf) {  // suspended: keep the search state resident
         heap_save(hp, lane);
         if (leader) {
-            ctl->best = sm.run_best;
+            ctl->best = best_r;
             ctl->iterations = it0 + it;
             __threadfence();
             ctl->life = LIFE_RUNNING;
@@ -554,45 +664,74 @@ __device__ void run_instance(const LaunchParams& P, const InstDesc& d, CtaShared
         return;
     }
     if (leader) {
-        ctl->best = sm.run_best;
+        ctl->best = best_r;
         ctl->iterations = it0 + it;
         ctl->status = status;
+        ctl->t_end = globaltimer_ns();
         __threadfence();
         ctl->life = LIFE_DONE;
     }
 }
 
 template <uint32_t KINDS>
-__device__ __forceinline__ void dispatch(const LaunchParams& P, CtaShared& sm) {
+__device__ __forceinline__ void dispatch(const LaunchParams& P, CtaShared& sm, const TeamRef tm) {
     switch (sm.desc.kind) {
         case KIND_SLIDING3:
-            if constexpr ((KINDS & kind_bit(KIND_SLIDING3)) != 0) run_instance<SlidingDom<3>>(P, sm.desc, sm, sm.ctx.s3);
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING3)) != 0) run_instance<SlidingDom<3>>(P, sm.desc, sm, sm.ctx.s3, tm);
             break;
         case KIND_SLIDING4:
-            if constexpr ((KINDS & kind_bit(KIND_SLIDING4)) != 0) run_instance<SlidingDom<4>>(P, sm.desc, sm, sm.ctx.s4);
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING4)) != 0) run_instance<SlidingDom<4>>(P, sm.desc, sm, sm.ctx.s4, tm);
             break;
         case KIND_SLIDING5:
-            if constexpr ((KINDS & kind_bit(KIND_SLIDING5)) != 0) run_instance<SlidingDom<5>>(P, sm.desc, sm, sm.ctx.s5);
+            if constexpr ((KINDS & kind_bit(KIND_SLIDING5)) != 0) run_instance<SlidingDom<5>>(P, sm.desc, sm, sm.ctx.s5, tm);
             break;
         case KIND_GRID:
-            if constexpr ((KINDS & kind_bit(KIND_GRID)) != 0) run_instance<GridDom>(P, sm.desc, sm, sm.ctx.g);
+            if constexpr ((KINDS & kind_bit(KIND_GRID)) != 0) run_instance<GridDom>(P, sm.desc, sm, sm.ctx.g, tm);
             break;
         default:
             break;
     }
 }
 
-// Persistent search kernel.  One-block teams take instances from a work
-// counter until none is left; a multi-block team (cooperative launch) runs
-// instance 0 on every block.
+// Persistent search kernel.
+//  * plain (team_ctas > 1): every block works on instance 0 (cooperative launch);
+//  * batch/serve: blocks of the heavy teams first take heavy instances together,
+//    then every block takes instances one block each from a work counter.
 template <uint32_t KINDS>
 __global__ void __launch_bounds__(512, 1) search_kernel(LaunchParams P) {
     __shared__ CtaShared sm;
     if (P.team_ctas > 1) {
         if (threadIdx.x == 0) sm.desc = P.insts[0];
         __syncthreads();
-        dispatch<KINDS>(P, sm);
+        dispatch<KINDS>(P, sm, TeamRef{P.team_ctas, blockIdx.x, P.team, P.stage});
         return;
+    }
+    if (P.n_heavy && blockIdx.x < P.heavy_teams * P.heavy_team) {
+        const uint32_t t = blockIdx.x / P.heavy_team, rank = blockIdx.x % P.heavy_team;
+        TeamCtl* tc = P.heavy_ctl + t;
+        const TeamRef tm{P.heavy_team, rank, tc,
+                         reinterpret_cast<char*>(P.heavy_stage) + (size_t)t * P.heavy_stage_bytes};
+        for (;;) {
+            // Every block of the team is done with the previous instance here.
+            if (!team_sync_grid(tc, P.heavy_team, P.barrier_timeout_ns, sm)) break;
+            if (rank == 0 && threadIdx.x == 0) {
+                for (uint32_t k = 0; k < kSlots; ++k) {
+                    tc->slot[k].minprio = kInfPrio;
+                    tc->slot[k].minstage = kInfPrio;
+                    tc->slot[k].count = 0;
+                    tc->slot[k].best = kInf;
+                    tc->slot[k].err = 0;
+                }
+                tc->inst = atomicAdd(P.heavy_next, 1u);
+            }
+            if (!team_sync_grid(tc, P.heavy_team, P.barrier_timeout_ns, sm)) break;
+            const uint32_t i = ld_vol(&tc->inst);
+            if (i >= P.n_heavy) break;
+            if (threadIdx.x == 0) sm.desc = P.insts[P.heavy_order[i]];
+            __syncthreads();
+            dispatch<KINDS>(P, sm, tm);
+        }
+        __syncthreads();
     }
     for (;;) {
         if (threadIdx.x == 0) sm.inst = atomicAdd(P.next, 1u);
@@ -601,7 +740,7 @@ __global__ void __launch_bounds__(512, 1) search_kernel(LaunchParams P) {
         if (i >= P.n_insts) break;
         if (threadIdx.x == 0) sm.desc = P.insts[P.order ? P.order[i] : i];
         __syncthreads();
-        dispatch<KINDS>(P, sm);
+        dispatch<KINDS>(P, sm, TeamRef{1, 0, nullptr, nullptr});
         __syncthreads();
     }
 }

@@ -1,0 +1,458 @@
+// Served GA*: a continuous-batching request loop.
+//
+// Requests (puzzles or grids) wait in a FIFO queue.  Each scheduling round
+// (gastar_serve_step) admits waiting requests while a device slot and enough
+// of the device-memory budget are free (partitions come from one arena of
+// `budget_bytes` through a first-fit allocator), then runs one persistent
+// launch over every active request for at most `slice_iters` GA* iterations
+// each.  The search state (table, warp-heaps, control block) stays resident
+// between rounds; finished requests get their path rebuilt, release their
+// partition and slot, and the next round admits new work into them.  So
+// requests that arrive while others are on the GPU join as capacity frees up,
+// and their iterations interleave with the running ones inside the same
+// launches.  A request whose partition overflows is re-queued at the front
+// with 4x larger partitions.
+//
+// The reference has no counterpart: it solves one instance per process.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gastar.h"
+#include "device_common.cuh"
+#include "engine_internal.h"
+#include "partition.h"
+
+using namespace gastar;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+// First-fit allocator over [0, size) with coalescing of free ranges.
+struct RangeAlloc {
+    std::map<uint64_t, uint64_t> free_;  // offset -> length
+    uint64_t in_use = 0;
+    void reset(uint64_t size) {
+        free_.clear();
+        if (size) free_[0] = size;
+        in_use = 0;
+    }
+    bool alloc(uint64_t n, uint64_t& off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < n) continue;
+            off = it->first;
+            const uint64_t rest = it->second - n;
+            free_.erase(it);
+            if (rest) free_[off + n] = rest;
+            in_use += n;
+            return true;
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t n) {
+        in_use -= n;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
+enum ReqState { WAITING = 0, ACTIVE = 1, DONE = 2 };
+
+struct Request {
+    Problem prob;
+    uint32_t retry_level = 0;
+    int state = WAITING;
+    int slot = -1;
+    uint64_t part_off = 0, part_bytes = 0;
+    Clock::time_point t_submit, t_done;
+    InstCtl ctl{};
+    uint64_t prior_expansions = 0;
+    uint32_t prior_iterations = 0;
+    std::vector<unsigned long long> path;  // goal first
+};
+
+}  // namespace
+
+struct gastar_server {
+    gastar_ctx* ctx = nullptr;
+    gastar_serve_config cfg;
+    DevBuf arena, descs, ctls, order, counters, path_descs, path_arena;
+    RangeAlloc alloc;
+    uint32_t max_active = 0, threads = 0;
+    size_t smem = 0;
+    std::vector<InstDesc> h_desc;
+    std::vector<int64_t> slot_req;
+    std::vector<int> free_slots;
+    InstCtl* h_ctl = nullptr;  // pinned, max_active
+    std::deque<int64_t> waiting;
+    std::unordered_map<int64_t, Request> reqs;
+    int64_t next_id = 0;
+    uint64_t completed = 0;
+    float kernel_ms = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level) {
+    PartConfig pc;
+    pc.warps = s->cfg.warps_per_block;
+    pc.ew = s->cfg.expansion_width;
+    pc.load_factor = s->cfg.load_factor;
+    pc.heuristic = s->cfg.heuristic;
+    pc.moves = s->cfg.moves;
+    pc.delta_grid = s->cfg.delta_grid;
+    pc.sliding_states = s->cfg.sliding_states;
+    pc.retry_level = retry_level;
+    pc.own_weights = true;
+    return pc;
+}
+
+void finish_request(gastar_server* s, Request& r, const InstCtl& c) {
+    r.ctl = c;
+    r.ctl.expansions += r.prior_expansions;
+    r.ctl.iterations += r.prior_iterations;
+    r.state = DONE;
+    r.t_done = Clock::now();
+    ++s->completed;
+}
+
+int64_t submit(gastar_server* s, Problem&& p) {
+    const int64_t id = s->next_id++;
+    Request r;
+    r.prob = std::move(p);
+    r.t_submit = Clock::now();
+    if (r.prob.unreachable) {
+        InstCtl c{};
+        c.status = ST_NO_PATH;
+        c.life = LIFE_DONE;
+        auto& ref = s->reqs.emplace(id, std::move(r)).first->second;
+        finish_request(s, ref, c);
+        return id;
+    }
+    s->reqs.emplace(id, std::move(r));
+    s->waiting.push_back(id);
+    return id;
+}
+
+// Admits waiting requests in arrival order while a slot and memory are free.
+int admit(gastar_server* s, cudaStream_t st) {
+    while (!s->waiting.empty() && !s->free_slots.empty()) {
+        const int64_t id = s->waiting.front();
+        Request& r = s->reqs[id];
+        const PartConfig pc = serve_part_config(s, r.retry_level);
+        const PartPlan plan = plan_partition(r.prob, pc);
+        if (plan.bytes > s->arena.n) {  // can never fit the budget
+            s->waiting.pop_front();
+            InstCtl c{};
+            c.status = GASTAR_OUT_OF_MEMORY;
+            c.life = LIFE_DONE;
+            finish_request(s, r, c);
+            continue;
+        }
+        uint64_t off;
+        if (!s->alloc.alloc(plan.bytes, off)) break;  // wait for memory to free up
+        s->waiting.pop_front();
+        const int slot = s->free_slots.back();
+        s->free_slots.pop_back();
+        r.slot = slot;
+        r.part_off = off;
+        r.part_bytes = plan.bytes;
+        r.state = ACTIVE;
+        s->slot_req[slot] = id;
+        char* base = reinterpret_cast<char*>(s->arena.p) + off;
+        InstCtl* ctl = reinterpret_cast<InstCtl*>(s->ctls.p) + slot;
+        fill_desc(s->h_desc[slot], r.prob, pc, plan, base, nullptr, ctl);
+        if (r.prob.kind == KIND_GRID &&
+            !cuda_ok(cudaMemcpyAsync(base + plan.weights_off, r.prob.weights.data(), r.prob.weights.size(),
+                                     cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+            return GASTAR_CUDA_ERROR;
+        if (!cuda_ok(cudaMemsetAsync(ctl, 0, sizeof(InstCtl), st), "cudaMemsetAsync") ||
+            !cuda_ok(cudaMemcpyAsync(reinterpret_cast<InstDesc*>(s->descs.p) + slot, &s->h_desc[slot],
+                                     sizeof(InstDesc), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+            return GASTAR_CUDA_ERROR;
+    }
+    return GASTAR_OK;
+}
+
+void release_slot(gastar_server* s, Request& r) {
+    s->alloc.release(r.part_off, r.part_bytes);
+    s->slot_req[r.slot] = -1;
+    s->free_slots.push_back(r.slot);
+    r.slot = -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gastar_serve_config_default(gastar_serve_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->budget_bytes = 120ull << 30;
+    c->slice_iters = 64;
+    c->warps_per_block = 8;
+    c->expansion_width = 32;
+    c->load_factor = 0.75f;
+    c->delta_grid = 36;
+}
+
+gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
+    if (!c) return nullptr;
+    if (cudaSetDevice(c->device) != cudaSuccess) return nullptr;
+    auto* s = new gastar_server();
+    s->ctx = c;
+    if (cfg) s->cfg = *cfg;
+    else gastar_serve_config_default(&s->cfg);
+    auto& cf = s->cfg;
+    if (!cf.warps_per_block) cf.warps_per_block = 8;
+    cf.warps_per_block = std::min(16u, cf.warps_per_block);
+    if (!cf.expansion_width) cf.expansion_width = 32;
+    cf.expansion_width = std::min(32u, cf.expansion_width);
+    if (cf.load_factor <= 0.f) cf.load_factor = 0.75f;
+    if (!cf.slice_iters) cf.slice_iters = 64;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    uint64_t budget = cf.budget_bytes ? cf.budget_bytes : (120ull << 30);
+    budget = std::min<uint64_t>(budget, free_b > (2ull << 30) ? free_b - (2ull << 30) : free_b / 2);
+    cf.budget_bytes = budget;
+    s->threads = cf.warps_per_block * 32;
+    s->smem = block_smem_bytes(kKindsAll, cf.warps_per_block, cf.expansion_width, false);
+    const int nb = occupancy_blocks(c, kKindsAll, s->threads, s->smem);
+    if (nb <= 0) {
+        delete s;
+        return nullptr;
+    }
+    s->max_active = cf.max_active ? cf.max_active : (uint32_t)(nb * c->sms);
+    const uint32_t m = s->max_active;
+    if (!s->arena.ensure(budget) || !s->descs.ensure(sizeof(InstDesc) * m) ||
+        !s->ctls.ensure(sizeof(InstCtl) * m) || !s->order.ensure(sizeof(uint32_t) * m) ||
+        !s->counters.ensure(64) ||
+        !cuda_ok(cudaMallocHost(&s->h_ctl, sizeof(InstCtl) * m), "cudaMallocHost")) {
+        gastar_serve_destroy(s);
+        return nullptr;
+    }
+    s->alloc.reset(s->arena.n);
+    s->h_desc.assign(m, InstDesc());
+    s->slot_req.assign(m, -1);
+    for (int i = (int)m - 1; i >= 0; --i) s->free_slots.push_back(i);
+    cudaEventCreate(&s->e0);
+    cudaEventCreate(&s->e1);
+    return s;
+}
+
+void gastar_serve_destroy(gastar_server* s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    s->arena.release();
+    s->descs.release();
+    s->ctls.release();
+    s->order.release();
+    s->counters.release();
+    s->path_descs.release();
+    s->path_arena.release();
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
+    if (s->e0) cudaEventDestroy(s->e0);
+    if (s->e1) cudaEventDestroy(s->e1);
+    delete s;
+}
+
+int64_t gastar_serve_submit_sliding(gastar_server* s, uint32_t n, const uint8_t* start, const uint8_t* goal) {
+    if (!s) return -GASTAR_BAD_INPUT;
+    Problem p;
+    if (!make_sliding_problem(n, start, goal, s->cfg.heuristic, s->cfg.moves, p)) {
+        set_error("sliding: boards must be permutations of 0..n*n-1 with n in 3..5");
+        return -GASTAR_BAD_INPUT;
+    }
+    return submit(s, std::move(p));
+}
+
+int64_t gastar_serve_submit_grid(gastar_server* s, uint32_t w, uint32_t h, const uint8_t* weights,
+                                 uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty) {
+    if (!s) return -GASTAR_BAD_INPUT;
+    Problem p;
+    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, s->cfg.heuristic, p)) {
+        set_error("grid: bad dimensions or endpoints");
+        return -GASTAR_BAD_INPUT;
+    }
+    return submit(s, std::move(p));
+}
+
+int gastar_serve_step(gastar_server* s) {
+    if (!s) return GASTAR_BAD_INPUT;
+    if (cudaSetDevice(s->ctx->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
+    cudaStream_t st = s->ctx->stream;
+    int rc = admit(s, st);
+    if (rc != GASTAR_OK) return rc;
+    std::vector<uint32_t> active;
+    for (uint32_t i = 0; i < s->max_active; ++i)
+        if (s->slot_req[i] >= 0) active.push_back(i);
+    if (active.empty()) return GASTAR_OK;
+    // Larger remaining work first inside the launch.
+    std::stable_sort(active.begin(), active.end(), [&](uint32_t a, uint32_t b) {
+        return s->reqs[s->slot_req[a]].prob.est > s->reqs[s->slot_req[b]].prob.est;
+    });
+    const uint32_t n = (uint32_t)active.size();
+    if (!cuda_ok(cudaMemcpyAsync(s->order.p, active.data(), 4ull * n, cudaMemcpyHostToDevice, st),
+                 "cudaMemcpyAsync") ||
+        !cuda_ok(cudaMemsetAsync(s->counters.p, 0, 16, st), "cudaMemsetAsync"))
+        return GASTAR_CUDA_ERROR;
+    LaunchParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.insts = reinterpret_cast<const InstDesc*>(s->descs.p);
+    P.n_insts = n;
+    P.order = reinterpret_cast<const uint32_t*>(s->order.p);
+    P.next = reinterpret_cast<uint32_t*>(s->counters.p);
+    P.team_ctas = 1;
+    P.slice_iters = s->cfg.slice_iters;
+    P.barrier_timeout_ns = 2000000000ull;
+    const uint32_t blocks = std::min(n, s->max_active);
+    cudaEventRecord(s->e0, st);
+    rc = launch_search(s->ctx, kKindsAll, P, blocks, s->threads, s->smem, st);
+    if (rc != GASTAR_OK) return rc;
+    cudaEventRecord(s->e1, st);
+    if (!cuda_ok(cudaMemcpyAsync(s->h_ctl, s->ctls.p, sizeof(InstCtl) * s->max_active,
+                                 cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync") ||
+        !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+        return GASTAR_CUDA_ERROR;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->e0, s->e1);
+    s->kernel_ms += ms;
+
+    // Retire finished requests: paths for the solved ones, re-queue overflows.
+    std::vector<uint32_t> solved;
+    std::vector<int64_t> requeue;
+    for (uint32_t slot : active) {
+        const InstCtl& c = s->h_ctl[slot];
+        if (c.life != LIFE_DONE) continue;
+        Request& r = s->reqs[s->slot_req[slot]];
+        if ((c.status == ST_TABLE_FULL || c.status == ST_HEAP_FULL) && r.retry_level < 3) {
+            r.prior_expansions += c.expansions;
+            r.prior_iterations += c.iterations;
+            r.retry_level += 1;
+            r.state = WAITING;
+            requeue.push_back(s->slot_req[slot]);
+            release_slot(s, r);
+            continue;
+        }
+        if (c.status == ST_OK) solved.push_back(slot);
+        else {
+            finish_request(s, r, c);
+            release_slot(s, r);
+        }
+    }
+    for (auto it = requeue.rbegin(); it != requeue.rend(); ++it) s->waiting.push_front(*it);
+    if (!solved.empty()) {
+        std::vector<InstDesc> pd;
+        uint64_t words = 0;
+        for (uint32_t slot : solved) {
+            pd.push_back(s->h_desc[slot]);
+            words += ((uint64_t)s->h_ctl[slot].best + 2) * key_words(s->h_desc[slot].kind);
+        }
+        const uint32_t m = (uint32_t)pd.size();
+        if (!s->path_descs.ensure(sizeof(InstDesc) * m) || !s->path_arena.ensure(words * 8 + 16))
+            return GASTAR_OUT_OF_MEMORY;
+        unsigned long long* used = reinterpret_cast<unsigned long long*>(s->counters.p) + 2;
+        if (!cuda_ok(cudaMemcpyAsync(s->path_descs.p, pd.data(), sizeof(InstDesc) * m,
+                                     cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
+            !cuda_ok(cudaMemsetAsync(used, 0, 8, st), "cudaMemsetAsync"))
+            return GASTAR_CUDA_ERROR;
+        rc = launch_paths(reinterpret_cast<const InstDesc*>(s->path_descs.p), m,
+                          reinterpret_cast<unsigned long long*>(s->path_arena.p), words, used, st);
+        if (rc != GASTAR_OK) return rc;
+        std::vector<unsigned long long> arena(words);
+        if (!cuda_ok(cudaMemcpyAsync(s->h_ctl, s->ctls.p, sizeof(InstCtl) * s->max_active,
+                                     cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync") ||
+            !cuda_ok(cudaMemcpyAsync(arena.data(), s->path_arena.p, words * 8, cudaMemcpyDeviceToHost, st),
+                     "cudaMemcpyAsync") ||
+            !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+            return GASTAR_CUDA_ERROR;
+        for (uint32_t slot : solved) {
+            const InstCtl& c = s->h_ctl[slot];
+            Request& r = s->reqs[s->slot_req[slot]];
+            if (c.status == ST_OK) {
+                const uint64_t w = (uint64_t)c.path_len * key_words(r.prob.kind);
+                r.path.assign(arena.begin() + c.path_off, arena.begin() + c.path_off + w);
+            }
+            finish_request(s, r, c);
+            release_slot(s, r);
+        }
+    }
+    return GASTAR_OK;
+}
+
+int gastar_serve_poll(gastar_server* s, int64_t id, gastar_result* out, void* path, uint32_t cap,
+                      uint32_t* len) {
+    if (!s || !out) return GASTAR_BAD_INPUT;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return GASTAR_BAD_INPUT;
+    const Request& r = it->second;
+    std::memset(out, 0, sizeof(*out));
+    if (r.state != DONE) {
+        out->status = GASTAR_PENDING;
+        return GASTAR_PENDING;
+    }
+    const InstCtl& c = r.ctl;
+    out->status = (int32_t)c.status;
+    out->cost = c.status == ST_OK ? c.best : 0;
+    out->path_len = c.status == ST_OK ? c.path_len : 0;
+    out->iterations = c.iterations;
+    out->expansions = c.expansions;
+    out->generated = c.generated;
+    out->pushes = c.pushes;
+    out->stale = c.stale;
+    out->table_used = c.table_used;
+    out->total_ms = std::chrono::duration<float, std::milli>(r.t_done - r.t_submit).count();
+    out->attempts = 1 + r.retry_level;
+    if (len) *len = out->path_len;
+    if (path && c.status == ST_OK) {
+        if (c.path_len > cap) return GASTAR_PATH_CAP;
+        const uint32_t kw = key_words(r.prob.kind);
+        for (uint32_t i = 0; i < c.path_len; ++i) {
+            const uint32_t j = c.path_len - 1 - i;  // stored goal-first
+            if (r.prob.kind == KIND_GRID) reinterpret_cast<uint32_t*>(path)[i] = (uint32_t)r.path[j];
+            else
+                unpack_board(r.prob.n, r.path[(size_t)j * kw], kw == 2 ? r.path[(size_t)j * kw + 1] : 0,
+                             reinterpret_cast<uint8_t*>(path) + (size_t)i * r.prob.n * r.prob.n);
+        }
+    }
+    return GASTAR_OK;
+}
+
+int gastar_serve_release(gastar_server* s, int64_t id) {
+    if (!s) return GASTAR_BAD_INPUT;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || it->second.state != DONE) return GASTAR_BAD_INPUT;
+    s->reqs.erase(it);
+    return GASTAR_OK;
+}
+
+int gastar_serve_stats(gastar_server* s, uint32_t* waiting, uint32_t* active, uint64_t* completed,
+                       uint64_t* bytes_in_use, float* kernel_ms) {
+    if (!s) return GASTAR_BAD_INPUT;
+    if (waiting) *waiting = (uint32_t)s->waiting.size();
+    if (active) *active = s->max_active - (uint32_t)s->free_slots.size();
+    if (completed) *completed = s->completed;
+    if (bytes_in_use) *bytes_in_use = s->alloc.in_use;
+    if (kernel_ms) *kernel_ms = s->kernel_ms;
+    return GASTAR_OK;
+}
+
+}  // extern "C"

@@ -81,8 +81,10 @@ typedef struct gastar_result {
     uint64_t pushes;           /* successors that improved the table and were queued */
     uint64_t stale;            /* pops discarded because the table held a lower g */
     uint64_t table_used;       /* states stored in the duplicate-detection table */
-    float kernel_ms;           /* device time of the search kernel(s), CUDA events */
-    float total_ms;            /* host wall time of the call */
+    float kernel_ms;           /* device time of the search kernel(s), CUDA events; batch
+                                  results: this instance's first-to-last iteration time */
+    float total_ms;            /* host wall time of the call; batch results: whole launch;
+                                  served results: submit -> completion */
     uint32_t attempts;         /* plain engine: solves run (1 + regrows) */
     uint32_t launches;         /* kernels this call launched */
     uint64_t h2d_bytes;        /* bytes copied host -> device by this call */
@@ -151,6 +153,11 @@ typedef struct gastar_batch_config {
     uint32_t timeout_ms;
     uint64_t max_expansions;   /* per instance */
     uint64_t sliding_states;   /* expected max states per puzzle instance (0 = by size) */
+    uint32_t delta_grid;       /* pop window for grid instances (0 = none) */
+    uint32_t heavy_team;       /* blocks per team for heavy instances (1 = no teams) */
+    uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
+    uint64_t promote_expansions; /* puzzles past this many expansions are re-solved by the
+                                    plain engine on the whole GPU (0 = never) */
 } gastar_batch_config;
 
 void gastar_batch_config_default(gastar_batch_config *cfg);
@@ -173,6 +180,46 @@ int gastar_batch_path(gastar_batch *b, uint32_t index, void *path, uint32_t path
 /* Device time of the last run's kernel(s) and the bytes copied each way. */
 int gastar_batch_stats(gastar_batch *b, float *kernel_ms, uint64_t *h2d_bytes,
                        uint64_t *d2h_bytes, uint64_t *device_bytes);
+
+/* ---- served GA*: continuous batching of solve requests ----
+ * No reference counterpart (one instance per process there).  Requests wait in
+ * a FIFO queue; each gastar_serve_step admits waiting requests while a slot
+ * and enough of the device-memory budget are free, runs one persistent launch
+ * over every active request for at most slice_iters GA* iterations each (search
+ * state stays resident between steps), rebuilds the paths of finished ones and
+ * frees their memory.  total_ms of a polled result is submit -> completion. */
+typedef struct gastar_server gastar_server;
+typedef struct gastar_serve_config {
+    uint64_t budget_bytes;     /* device bytes for request partitions (default 120 GiB) */
+    uint32_t max_active;       /* requests on the device at once (0 = resident blocks) */
+    uint32_t slice_iters;      /* iterations per request per step */
+    uint32_t warps_per_block;  /* warp-heaps per request */
+    uint32_t expansion_width;  /* pops per warp-heap per iteration */
+    float load_factor;
+    uint32_t heuristic, moves;
+    uint32_t delta_grid;       /* pop window for grid requests (0 = none) */
+    uint64_t sliding_states;   /* expected max states per puzzle request (0 = by size) */
+} gastar_serve_config;
+
+void gastar_serve_config_default(gastar_serve_config *cfg);
+gastar_server *gastar_serve_create(gastar_ctx *ctx, const gastar_serve_config *cfg);
+void gastar_serve_destroy(gastar_server *srv);
+/* Returns a request id (>= 0) or a negative gastar_status. */
+int64_t gastar_serve_submit_sliding(gastar_server *srv, uint32_t n, const uint8_t *start,
+                                    const uint8_t *goal);
+int64_t gastar_serve_submit_grid(gastar_server *srv, uint32_t w, uint32_t h,
+                                 const uint8_t *weights, uint32_t sx, uint32_t sy, uint32_t tx,
+                                 uint32_t ty);
+/* One scheduling round: admit, one slice launch, retire finished requests. */
+int gastar_serve_step(gastar_server *srv);
+/* GASTAR_OK with the result (and path: boards or cell indices) when the
+ * request is finished, GASTAR_PENDING otherwise. */
+int gastar_serve_poll(gastar_server *srv, int64_t id, gastar_result *out, void *path,
+                      uint32_t path_cap, uint32_t *path_len);
+/* Forgets a finished request. */
+int gastar_serve_release(gastar_server *srv, int64_t id);
+int gastar_serve_stats(gastar_server *srv, uint32_t *waiting, uint32_t *active,
+                       uint64_t *completed, uint64_t *bytes_in_use, float *kernel_ms);
 
 /* ---- text formats and synthetic instances (host only, no GPU needed) ---- */
 /* Reads "start goal" in the reference's sliding format (Position(std::istream&),

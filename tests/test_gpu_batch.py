@@ -57,3 +57,50 @@ def test_batch_equals_plain(engine, gastar):
     for i, (s, g) in enumerate(inst):
         assert b.result(i, path=False).cost == engine.solve_sliding(s, g, 4, path=False).cost
     b.close()
+
+
+def test_batch_partition_overflow_is_retried(engine, oracle, gastar):
+    """Partitions sized far below the need overflow; the instances are
+    re-solved with larger partitions and still match the oracle."""
+    b = engine.batch(warps_per_block=4, expansion_width=32, sliding_states=4096)
+    inst = [gastar.gen_sliding(4, 1300 + i, 25, 40) for i in range(6)]
+    for s, g in inst:
+        b.add_sliding(s, g)
+    b.run()
+    for i, (s, g) in enumerate(inst):
+        r = b.result(i)
+        o, _ = oracle.sliding_astar(4, s, g, path=False)
+        assert r.status_name == "OK" and r.cost == o.cost
+        assert oracle.sliding_validate(4, s, g, r.path) == (True, r.cost)
+    b.close()
+
+
+def test_heavy_teams_and_promotion(engine, oracle, gastar):
+    """Large grids run on multi-block teams, and a puzzle past its expansion
+    budget is re-solved by the plain engine; all results match the oracle."""
+    b = engine.batch(warps_per_block=4, expansion_width=32, heavy_team=2, heavy_cells=200 * 200,
+                     promote_expansions=2000)
+    cases = []
+    for i in range(6):
+        side = 180 + 40 * i
+        wts = gastar.gen_grid(side, side, 1400 + i, 0.2)
+        cases.append(("g", wts, b.add_grid(wts, (0, 0), (side - 1, side - 1)), side))
+    for i in range(6):
+        s, g = gastar.gen_sliding(4, 1500 + i, 30, 50)
+        cases.append(("s", (s, g), b.add_sliding(s, g), 0))
+    b.run()
+    for kind, a, idx, side in cases:
+        r = b.result(idx)
+        if kind == "g":
+            o, _ = oracle.grid_astar(a, (0, 0), (side - 1, side - 1), path=False)
+            assert r.status_name == "OK" and r.cost == o.cost
+            assert oracle.grid_validate(a, (0, 0), (side - 1, side - 1), r.path) == (True, r.cost)
+        else:
+            s, g = a
+            o, _ = oracle.sliding_astar(4, s, g, path=False)
+            assert r.status_name == "OK" and r.cost == o.cost
+            assert oracle.sliding_validate(4, s, g, r.path) == (True, r.cost)
+    b.rerun()
+    for kind, a, idx, side in cases:
+        assert b.result(idx, path=False).status_name == "OK"
+    b.close()

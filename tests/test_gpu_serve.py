@@ -1,0 +1,75 @@
+"""Served GA*: continuous batching gives the same results alone and in a mix."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _mix(gastar, k):
+    rng = np.random.default_rng(99)
+    reqs = []
+    for i in range(k):
+        kind = i % 4
+        if kind == 0:
+            reqs.append(("s", *gastar.gen_sliding(3, 4000 + i, 60, 60)))
+        elif kind == 1:
+            reqs.append(("s", *gastar.gen_sliding(4, 4100 + i, 20, 50)))
+        elif kind == 2:
+            reqs.append(("s", *gastar.gen_sliding(5, 4200 + i, 10, 20)))
+        else:
+            side = int(rng.integers(64, 400))
+            wts = gastar.gen_grid(side, side + 3, 4300 + i, 0.2)
+            reqs.append(("g", wts, (0, 0), (side - 1, side + 2)))
+    return reqs
+
+
+def _submit(srv, r):
+    return srv.submit_sliding(r[1], r[2]) if r[0] == "s" else srv.submit_grid(r[1], r[2], r[3])
+
+
+def _check(oracle, r, res):
+    if r[0] == "s":
+        n = int(round(len(r[1]) ** 0.5))
+        o, _ = oracle.sliding_astar(n, r[1], r[2], path=False)
+        assert res.status_name == "OK" and res.cost == o.cost
+        assert oracle.sliding_validate(n, r[1], r[2], res.path) == (True, res.cost)
+    else:
+        o, _ = oracle.grid_astar(r[1], r[2], r[3], path=False)
+        assert res.status_name == "OK" and res.cost == o.cost
+        assert oracle.grid_validate(r[1], r[2], r[3], res.path) == (True, res.cost)
+
+
+def test_results_same_alone_and_in_mix(engine, oracle, gastar):
+    reqs = _mix(gastar, 24)
+    srv = engine.server(slice_iters=16, budget_bytes=8 << 30)
+    # Staggered arrivals: a third before the first step, the rest while running.
+    ids = [_submit(srv, r) for r in reqs[:8]]
+    srv.step()
+    ids += [_submit(srv, r) for r in reqs[8:16]]
+    srv.step()
+    ids += [_submit(srv, r) for r in reqs[16:]]
+    mixed = srv.drain(ids)
+    srv.close()
+    for r, i in zip(reqs, ids):
+        _check(oracle, r, mixed[i])
+    # The same requests one at a time.
+    for r, i in zip(reqs, ids):
+        one = engine.server(slice_iters=16, budget_bytes=2 << 30)
+        j = _submit(one, r)
+        alone = one.drain([j])[j]
+        one.close()
+        assert (alone.status, alone.cost) == (mixed[i].status, mixed[i].cost)
+
+
+def test_budget_limits_admission(engine, oracle, gastar):
+    """A small budget admits few requests at a time; all still finish."""
+    srv = engine.server(slice_iters=32, budget_bytes=256 << 20)
+    reqs = [("s", *gastar.gen_sliding(4, 5000 + i, 20, 40)) for i in range(12)]
+    ids = [_submit(srv, r) for r in reqs]
+    srv.step()
+    st = srv.stats()
+    assert st["active"] < 12 and st["waiting"] > 0
+    out = srv.drain(ids)
+    for r, i in zip(reqs, ids):
+        _check(oracle, r, out[i])
+    srv.close()
