@@ -112,6 +112,95 @@ class Clocks:
                 "samples": len(sm)}
 
 
+MIXED = {
+    "name": "Batched GA*: 1024 mixed instances in one persistent launch -- 512 15-puzzles "
+            "(random walk 20-80) + 512 weighted grids (side 256-2048, weights 1-9, obstacle "
+            "density 0.1-0.3, corridor-guaranteed path)",
+    "p15": 512, "grids": 512, "walk": (20, 80), "side": (256, 2048), "density": (0.1, 0.3),
+    "seed0": 0x3_0000,
+}
+
+
+def _mixed_instances(g):
+    import numpy as np
+    rng = np.random.default_rng(MIXED["seed0"])
+    p15 = [g.gen_sliding(4, MIXED["seed0"] + i, *MIXED["walk"]) for i in range(MIXED["p15"])]
+    grids = []
+    for i in range(MIXED["grids"]):
+        side = int(rng.integers(MIXED["side"][0], MIXED["side"][1] + 1))
+        dens = float(rng.uniform(*MIXED["density"]))
+        grids.append((g.gen_grid(side, side, MIXED["seed0"] + 100_000 + i, dens), side))
+    return p15, grids
+
+
+def run_batched(g, eng, steps: int) -> dict:
+    """configs[3]: one persistent launch over 1024 mixed instances (autotuned),
+    against the plain engine on a stratified 64-instance sample of the mix."""
+    import numpy as np
+    p15, grids = _mixed_instances(g)
+
+    def fill(b):
+        for s, goal in p15:
+            b.add_sliding(s, goal)
+        for w, side in grids:
+            b.add_grid(w, (0, 0), (side - 1, side - 1))
+
+    tuner = eng.batch()
+    fill(tuner)
+    cache = os.path.join(ROOT, "gpurun_out", "autotune_cache.txt") if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else None
+    t0 = time.perf_counter()
+    tuned = tuner.autotune(sample=64, cache_path=cache)
+    tune_s = time.perf_counter() - t0
+    tuner.close()
+    cfgkw = {k: tuned[k] for k in ("warps_per_block", "expansion_width", "load_factor",
+                                    "delta_grid", "heavy_team")}
+    # end to end: host buffers -> upload -> solve -> results and paths back
+    t0 = time.perf_counter()
+    b = eng.batch(**cfgkw)
+    fill(b)
+    b.run()
+    res = [b.result(i, path=True) for i in range(len(b))]
+    e2e_s = time.perf_counter() - t0
+    st0 = b.stats()
+    # device-resident reruns (graph replay)
+    kms = []
+    for _ in range(steps):
+        b.rerun()
+        kms.append(b.stats()["kernel_ms"])
+    res = [b.result(i, path=False) for i in range(len(b))]
+    n = len(res)
+    ok = sum(1 for r in res if r.status == g.OK)
+    exp = sum(r.expansions for r in res)
+    ms = statistics.median(kms)
+    lat = sorted(r.kernel_ms for r in res)
+    b.close()
+    # plain engine, one instance per launch, on a stratified sample of the mix
+    sample = list(range(0, len(p15), 16)) + [len(p15) + i for i in range(0, len(grids), 16)]
+    t_plain = 0.0
+    for i in sample:
+        if i < len(p15):
+            r = eng.solve_sliding(*p15[i], 4, num_queues=16384, path=True, path_cap=1024)
+        else:
+            w, side = grids[i - len(p15)]
+            r = eng.solve_grid(w, (0, 0), (side - 1, side - 1), num_queues=16384, delta=36, path=True)
+        t_plain += r.total_ms / 1000.0
+    plain_sps = len(sample) / t_plain
+    return {
+        "workload": MIXED["name"], "instances": n, "solved": ok,
+        "solves_per_s": n / (ms / 1000.0), "node_expansions_per_s": exp / (ms / 1000.0),
+        "ms_per_step": ms, "e2e_solves_per_s": n / e2e_s,
+        "e2e_h2d_bytes": st0["h2d_bytes"], "e2e_d2h_bytes": st0["d2h_bytes"],
+        "device_bytes": st0["device_bytes"],
+        "instance_device_ms": {"p50": lat[n // 2], "p99": lat[min(n - 1, int(n * 0.99))],
+                               "max": lat[-1]},
+        "autotuned": cfgkw, "autotune_s": tune_s,
+        "plain_same_mix_solves_per_s": plain_sps,
+        "plain_sample": f"{len(sample)} instances (every 16th of each class), one per launch",
+        "batched_over_plain": (n / (ms / 1000.0)) / plain_sps,
+    }
+
+
 def run_reference(args) -> dict:
     """The CPU implementation of the path (host A*, all host threads)."""
     import cuda_a_star_gb300 as g
@@ -249,6 +338,8 @@ def run_ours(args) -> dict:
                                "sample": f"the same {n_inst} instances once, single-thread host "
                                          f"A* per instance over {used} threads"}
         out["optimal_cost_agreement"] = agree
+    if rank == 0 and world == 1 and not args.no_batched:
+        out["batched"] = run_batched(g, eng, max(1, min(args.steps, 3)))
     if world > 1:
         torch.distributed.destroy_process_group()
     eng.close()
@@ -277,6 +368,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched mixed workload")
     ap.add_argument("--profile-case", action="store_true",
                     help="small single pass for ncu captures (no JSON line)")
     args = ap.parse_args()

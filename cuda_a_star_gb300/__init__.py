@@ -214,6 +214,18 @@ class Batch:
         self.kinds.append(("grid", w * h))
         return i
 
+    def autotune(self, sample: int = 64, cache_path: str | None = None) -> dict:
+        """Picks the batch configuration for this instance mix (before run())."""
+        out = BatchConfig()
+        ms = C.c_float()
+        _check(lib().gastar_batch_autotune(self._h, sample,
+                                           cache_path.encode() if cache_path else None,
+                                           C.byref(out), C.byref(ms)), "gastar_batch_autotune")
+        self.cfg = out
+        return {"warps_per_block": out.warps_per_block, "expansion_width": out.expansion_width,
+                "load_factor": round(out.load_factor, 3), "delta_grid": out.delta_grid,
+                "heavy_team": out.heavy_team, "trial_ms": ms.value}
+
     def run(self) -> None:
         _check(lib().gastar_batch_run(self._h), "gastar_batch_run")
 

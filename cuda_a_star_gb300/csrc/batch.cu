@@ -12,8 +12,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "../../include/gastar.h"
@@ -575,3 +577,143 @@ int gastar_batch_stats(gastar_batch* b, float* kernel_ms, uint64_t* h2d, uint64_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner: picks queue count (warp-heaps per instance), expansion width,
+// table load factor, grid pop window and heavy-team size for the instance mix
+// of a batch by timing trial batches over a stratified sample of its
+// instances (coordinate descent from the current configuration).  Results are
+// cached per GPU and mix signature in a text file.
+// ---------------------------------------------------------------------------
+namespace {
+
+std::string mix_signature(const gastar_batch* b) {
+    uint64_t counts[4] = {0, 0, 0, 0}, cells = 0, big = 0;
+    for (const Problem& p : b->insts) {
+        counts[p.kind] += 1;
+        if (p.kind == KIND_GRID) {
+            cells += (uint64_t)p.W * p.H;
+            big += (uint64_t)p.W * p.H >= b->cfg.heavy_cells;
+        }
+    }
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s|sm%d|s3:%llu|s4:%llu|s5:%llu|g:%llu|cells:%llu|big:%llu|h%u|m%u",
+                  b->ctx->name, b->ctx->sms, (unsigned long long)counts[0], (unsigned long long)counts[1],
+                  (unsigned long long)counts[2], (unsigned long long)counts[3],
+                  (unsigned long long)(counts[3] ? cells / counts[3] : 0), (unsigned long long)big,
+                  b->cfg.heuristic, b->cfg.moves);
+    for (char* c = buf; *c; ++c)
+        if (*c == ' ' || *c == '\t') *c = '_';
+    return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& sig, gastar_batch_config& cfg) {
+    if (!path) return false;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        char key[600];
+        unsigned w, ew, dg, team;
+        float lf;
+        if (std::sscanf(line, "%599s %u %u %f %u %u", key, &w, &ew, &lf, &dg, &team) == 6 && sig == key) {
+            cfg.warps_per_block = w;
+            cfg.expansion_width = ew;
+            cfg.load_factor = lf;
+            cfg.delta_grid = dg;
+            cfg.heavy_team = team;
+            found = true;  // the last matching line wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+// Device time of one trial batch over `idx` with configuration `cfg`.
+int trial(gastar_batch* b, const std::vector<uint32_t>& idx, const gastar_batch_config& cfg, float& ms) {
+    gastar_batch* t = gastar_batch_create(b->ctx, &cfg);
+    if (!t) return GASTAR_OUT_OF_MEMORY;
+    t->cfg.use_graph = 0;
+    for (uint32_t i : idx) t->insts.push_back(b->insts[i]);
+    const int rc = gastar_batch_run(t);
+    ms = t->kernel_ms;
+    for (uint32_t j = 0; rc == GASTAR_OK && j < idx.size(); ++j)
+        if (t->h_ctl[j].status != ST_OK && t->h_ctl[j].status != ST_NO_PATH) ms = 1e30f;  // unusable
+    gastar_batch_destroy(t);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const char* cache_path,
+                                     gastar_batch_config* out, float* best_ms) {
+    if (!b || b->uploaded || b->insts.empty()) return GASTAR_BAD_INPUT;
+    const std::string sig = mix_signature(b);
+    gastar_batch_config best = b->cfg;
+    if (cache_lookup(cache_path, sig, best)) {
+        b->cfg = best;
+        if (out) *out = best;
+        if (best_ms) *best_ms = 0.f;
+        return GASTAR_OK;
+    }
+    // Stratified sample: every k-th instance in estimated-work order.
+    std::vector<uint32_t> all(b->insts.size());
+    std::iota(all.begin(), all.end(), 0u);
+    std::stable_sort(all.begin(), all.end(),
+                     [&](uint32_t x, uint32_t y) { return b->insts[x].est > b->insts[y].est; });
+    const uint32_t m = std::max(1u, std::min<uint32_t>(sample ? sample : 64, (uint32_t)all.size()));
+    std::vector<uint32_t> idx;
+    for (uint32_t j = 0; j < m; ++j) idx.push_back(all[(size_t)j * all.size() / m]);
+    bool grids = false, heavy = false;
+    for (uint32_t i : idx) {
+        grids |= b->insts[i].kind == KIND_GRID;
+        heavy |= b->insts[i].kind == KIND_GRID &&
+                 (uint64_t)b->insts[i].W * b->insts[i].H >= b->cfg.heavy_cells;
+    }
+    float best_t = 0;
+    int rc = trial(b, idx, best, best_t);
+    if (rc != GASTAR_OK) return rc;
+    auto try_values = [&](auto setter, std::initializer_list<double> values) -> int {
+        for (double v : values) {
+            gastar_batch_config c = best;
+            setter(c, v);
+            if (std::memcmp(&c, &best, sizeof(c)) == 0) continue;
+            float t = 0;
+            const int r = trial(b, idx, c, t);
+            if (r == GASTAR_OUT_OF_MEMORY) continue;
+            if (r != GASTAR_OK) return r;
+            if (t < best_t) {
+                best_t = t;
+                best = c;
+            }
+        }
+        return GASTAR_OK;
+    };
+    if ((rc = try_values([](gastar_batch_config& c, double v) { c.warps_per_block = (uint32_t)v; },
+                         {4, 8, 16})) != GASTAR_OK)
+        return rc;
+    if ((rc = try_values([](gastar_batch_config& c, double v) { c.expansion_width = (uint32_t)v; },
+                         {16, 32})) != GASTAR_OK)
+        return rc;
+    if (grids && (rc = try_values([](gastar_batch_config& c, double v) { c.delta_grid = (uint32_t)v; },
+                                  {18, 36, 72})) != GASTAR_OK)
+        return rc;
+    if (heavy && (rc = try_values([](gastar_batch_config& c, double v) { c.heavy_team = (uint32_t)v; },
+                                  {1, 2, 4, 8})) != GASTAR_OK)
+        return rc;
+    if ((rc = try_values([](gastar_batch_config& c, double v) { c.load_factor = (float)v; },
+                         {0.5, 0.7, 0.85})) != GASTAR_OK)
+        return rc;
+    b->cfg = best;
+    if (cache_path) {
+        if (FILE* f = std::fopen(cache_path, "a")) {
+            std::fprintf(f, "%s %u %u %.3f %u %u\n", sig.c_str(), best.warps_per_block, best.expansion_width,
+                         best.load_factor, best.delta_grid, best.heavy_team);
+            std::fclose(f);
+        }
+    }
+    if (out) *out = best;
+    if (best_ms) *best_ms = best_t;
+    return GASTAR_OK;
+}

@@ -177,6 +177,14 @@ int gastar_batch_result(gastar_batch *b, uint32_t index, gastar_result *out);
 /* Copies the path of one solved instance: boards (sliding) or cell indices (grid). */
 int gastar_batch_path(gastar_batch *b, uint32_t index, void *path, uint32_t path_cap,
                       uint32_t *path_len);
+/* Autotuner: times trial batches over a stratified sample of `sample`
+ * instances of this (not yet run) batch and keeps the fastest warp-heaps per
+ * instance, expansion width, grid pop window, heavy-team size and table load
+ * factor (coordinate descent).  The choice is applied to the batch, written
+ * to `out` and cached per GPU and instance-mix signature in `cache_path`
+ * (NULL = no cache); a cached signature skips the trials. */
+int gastar_batch_autotune(gastar_batch *b, uint32_t sample, const char *cache_path,
+                          gastar_batch_config *out, float *best_ms);
 /* Device time of the last run's kernel(s) and the bytes copied each way. */
 int gastar_batch_stats(gastar_batch *b, float *kernel_ms, uint64_t *h2d_bytes,
                        uint64_t *d2h_bytes, uint64_t *device_bytes);
