@@ -201,6 +201,88 @@ def run_batched(g, eng, steps: int) -> dict:
     }
 
 
+SERVED = {
+    "name": "Served GA*: Poisson arrivals of mixed requests -- 8-puzzles (walk 60), 15-puzzles "
+            "(walk 20-80), 24-puzzles (walk 20-40), weighted grids (side 512-8192, weights 1-9, "
+            "20% obstacles); 120 GiB device budget for request partitions",
+    "requests": 48, "loads": (0.5, 0.9, 1.2), "seed0": 0x5_0000,
+}
+
+
+def _served_requests(g):
+    import numpy as np
+    rng = np.random.default_rng(SERVED["seed0"])
+    reqs = []
+    for i in range(SERVED["requests"]):
+        k = i % 4
+        seed = SERVED["seed0"] + i
+        if k == 0:
+            reqs.append(("s", *g.gen_sliding(3, seed, 60, 60)))
+        elif k == 1:
+            reqs.append(("s", *g.gen_sliding(4, seed, 20, 80)))
+        elif k == 2:
+            reqs.append(("s", *g.gen_sliding(5, seed, 20, 40)))
+        else:
+            side = int(rng.integers(512, 8193))
+            w = g.gen_grid(side, side, seed, 0.2)
+            reqs.append(("g", w, (0, 0), (side - 1, side - 1)))
+    return reqs
+
+
+def run_served(g, eng) -> dict:
+    """configs[4]: the continuous-batching server under Poisson arrivals at
+    three offered loads, calibrated to its capacity on a burst of the mix."""
+    import numpy as np
+    reqs = _served_requests(g)
+    srv = eng.server(budget_bytes=120 << 30)
+
+    def submit(r):
+        return srv.submit_sliding(r[1], r[2]) if r[0] == "s" else srv.submit_grid(r[1], r[2], r[3])
+
+    def run(arrivals):
+        t0 = time.perf_counter()
+        ids, res, nxt = {}, {}, 0
+        order = np.argsort(arrivals)
+        while len(res) < len(reqs):
+            now = time.perf_counter() - t0
+            while nxt < len(order) and arrivals[order[nxt]] <= now:
+                ids[submit(reqs[order[nxt]])] = order[nxt]
+                nxt += 1
+            st = srv.stats()
+            if st["active"] or st["waiting"]:
+                srv.step()
+            elif nxt < len(order):
+                time.sleep(max(0.0, min(0.002, arrivals[order[nxt]] - now)))
+            for i in list(ids):
+                if i not in res:
+                    r = srv.poll(i, path=False)
+                    if r is not None:
+                        res[i] = r
+        wall = time.perf_counter() - t0
+        for i in ids:
+            srv.release(i)
+        lat = sorted(r.total_ms for r in res.values())
+        n = len(lat)
+        return {"solves_per_s": n / wall, "wall_s": wall,
+                "node_expansions_per_s": sum(r.expansions for r in res.values()) / wall,
+                "latency_ms": {"p50": lat[n // 2], "p99": lat[min(n - 1, int(n * 0.99))]},
+                "solved": sum(1 for r in res.values() if r.status == g.OK)}
+
+    burst = run(np.zeros(len(reqs)))
+    cap = burst["solves_per_s"]
+    rng = np.random.default_rng(SERVED["seed0"] + 1)
+    loads = {}
+    for f in SERVED["loads"]:
+        rate = f * cap
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
+        out = run(arrivals)
+        out["offered_per_s"] = rate
+        loads[f"{f}x"] = out
+    srv.close()
+    return {"workload": SERVED["name"], "requests": len(reqs), "capacity_solves_per_s": cap,
+            "burst": burst, "loads": loads}
+
+
 def run_reference(args) -> dict:
     """The CPU implementation of the path (host A*, all host threads)."""
     import cuda_a_star_gb300 as g
@@ -340,6 +422,8 @@ def run_ours(args) -> dict:
         out["optimal_cost_agreement"] = agree
     if rank == 0 and world == 1 and not args.no_batched:
         out["batched"] = run_batched(g, eng, max(1, min(args.steps, 3)))
+    if rank == 0 and world == 1 and not args.no_served:
+        out["served"] = run_served(g, eng)
     if world > 1:
         torch.distributed.destroy_process_group()
     eng.close()
@@ -369,6 +453,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched mixed workload")
+    ap.add_argument("--no-served", action="store_true", help="skip the served workload")
     ap.add_argument("--profile-case", action="store_true",
                     help="small single pass for ncu captures (no JSON line)")
     args = ap.parse_args()

@@ -68,6 +68,7 @@ class ServeConfig(C.Structure):
         ("warps_per_block", C.c_uint32), ("expansion_width", C.c_uint32),
         ("load_factor", C.c_float), ("heuristic", C.c_uint32), ("moves", C.c_uint32),
         ("delta_grid", C.c_uint32), ("sliding_states", C.c_uint64),
+        ("heavy_team", C.c_uint32), ("heavy_teams", C.c_uint32), ("heavy_cells", C.c_uint64),
     ]
 
 

@@ -56,7 +56,7 @@ PartPlan plan_partition(const Problem& p, const PartConfig& c) {
         pl.table_words = cells;
         pl.table_limit = ~0ull;
         table_bytes = cells * 8;
-        entries = std::max<uint64_t>(1 << 16, cells) << (2 * c.retry_level);
+        entries = std::max<uint64_t>(1 << 16, cells / 2) << (2 * c.retry_level);
         pl.path_words = std::max<uint64_t>(1024, 4ull * (p.W + p.H)) << c.retry_level;
     } else {
         uint64_t states = c.sliding_states ? c.sliding_states : (p.n == 3 ? 181440ull : (1ull << 20));

@@ -77,6 +77,7 @@ enum ReqState { WAITING = 0, ACTIVE = 1, DONE = 2 };
 
 struct Request {
     Problem prob;
+    bool heavy = false;  // runs on a multi-block team
     uint32_t retry_level = 0;
     int state = WAITING;
     int slot = -1;
@@ -93,7 +94,9 @@ struct Request {
 struct gastar_server {
     gastar_ctx* ctx = nullptr;
     gastar_serve_config cfg;
-    DevBuf arena, descs, ctls, order, counters, path_descs, path_arena;
+    DevBuf arena, descs, ctls, order, counters, path_descs, path_arena, team_ctl, team_stage;
+    uint32_t heavy_teams = 0;
+    uint64_t heavy_stage_bytes = 0;
     RangeAlloc alloc;
     uint32_t max_active = 0, threads = 0;
     size_t smem = 0;
@@ -111,9 +114,9 @@ struct gastar_server {
 
 namespace {
 
-PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level) {
+PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool heavy) {
     PartConfig pc;
-    pc.warps = s->cfg.warps_per_block;
+    pc.warps = s->cfg.warps_per_block * (heavy ? s->cfg.heavy_team : 1);
     pc.ew = s->cfg.expansion_width;
     pc.load_factor = s->cfg.load_factor;
     pc.heuristic = s->cfg.heuristic;
@@ -139,6 +142,8 @@ int64_t submit(gastar_server* s, Problem&& p) {
     Request r;
     r.prob = std::move(p);
     r.t_submit = Clock::now();
+    r.heavy = s->heavy_teams && r.prob.kind == KIND_GRID &&
+              (uint64_t)r.prob.W * r.prob.H >= s->cfg.heavy_cells;
     if (r.prob.unreachable) {
         InstCtl c{};
         c.status = ST_NO_PATH;
@@ -157,7 +162,7 @@ int admit(gastar_server* s, cudaStream_t st) {
     while (!s->waiting.empty() && !s->free_slots.empty()) {
         const int64_t id = s->waiting.front();
         Request& r = s->reqs[id];
-        const PartConfig pc = serve_part_config(s, r.retry_level);
+        const PartConfig pc = serve_part_config(s, r.retry_level, r.heavy);
         const PartPlan plan = plan_partition(r.prob, pc);
         if (plan.bytes > s->arena.n) {  // can never fit the budget
             s->waiting.pop_front();
@@ -210,7 +215,9 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     c->warps_per_block = 8;
     c->expansion_width = 32;
     c->load_factor = 0.75f;
-    c->delta_grid = 36;
+    c->delta_grid = 18;
+    c->heavy_team = 4;
+    c->heavy_cells = 1ull << 20;
 }
 
 gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
@@ -239,8 +246,19 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
         delete s;
         return nullptr;
     }
-    s->max_active = cf.max_active ? cf.max_active : (uint32_t)(nb * c->sms);
+    const uint32_t resident = (uint32_t)(nb * c->sms);
+    s->max_active = cf.max_active ? cf.max_active : resident;
     const uint32_t m = s->max_active;
+    if (!cf.heavy_team) cf.heavy_team = 1;
+    if (cf.heavy_team > 1) {
+        s->heavy_teams = cf.heavy_teams ? cf.heavy_teams : std::max(1u, resident / 4 / cf.heavy_team);
+        s->heavy_teams = std::min(s->heavy_teams, resident / cf.heavy_team);
+        s->heavy_stage_bytes =
+            2 * stage_entries_per_buffer(cf.warps_per_block * cf.heavy_team, cf.expansion_width, 8) * 16;
+        if (!s->heavy_teams || !s->team_ctl.ensure(sizeof(TeamCtl) * s->heavy_teams) ||
+            !s->team_stage.ensure(s->heavy_stage_bytes * s->heavy_teams))
+            s->heavy_teams = 0;
+    }
     if (!s->arena.ensure(budget) || !s->descs.ensure(sizeof(InstDesc) * m) ||
         !s->ctls.ensure(sizeof(InstCtl) * m) || !s->order.ensure(sizeof(uint32_t) * m) ||
         !s->counters.ensure(64) ||
@@ -268,6 +286,8 @@ void gastar_serve_destroy(gastar_server* s) {
     s->counters.release();
     s->path_descs.release();
     s->path_arena.release();
+    s->team_ctl.release();
+    s->team_stage.release();
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
     if (s->e0) cudaEventDestroy(s->e0);
     if (s->e1) cudaEventDestroy(s->e1);
@@ -301,29 +321,51 @@ int gastar_serve_step(gastar_server* s) {
     cudaStream_t st = s->ctx->stream;
     int rc = admit(s, st);
     if (rc != GASTAR_OK) return rc;
-    std::vector<uint32_t> active;
+    std::vector<uint32_t> active, light, heavy;
     for (uint32_t i = 0; i < s->max_active; ++i)
-        if (s->slot_req[i] >= 0) active.push_back(i);
+        if (s->slot_req[i] >= 0) {
+            active.push_back(i);
+            (s->reqs[s->slot_req[i]].heavy ? heavy : light).push_back(i);
+        }
     if (active.empty()) return GASTAR_OK;
-    // Larger remaining work first inside the launch.
-    std::stable_sort(active.begin(), active.end(), [&](uint32_t a, uint32_t b) {
+    // Larger remaining work first inside the launch; the order array holds the
+    // one-block requests, then the heavy ones.
+    auto by_est = [&](uint32_t a, uint32_t b) {
         return s->reqs[s->slot_req[a]].prob.est > s->reqs[s->slot_req[b]].prob.est;
-    });
-    const uint32_t n = (uint32_t)active.size();
-    if (!cuda_ok(cudaMemcpyAsync(s->order.p, active.data(), 4ull * n, cudaMemcpyHostToDevice, st),
+    };
+    std::stable_sort(light.begin(), light.end(), by_est);
+    std::stable_sort(heavy.begin(), heavy.end(), by_est);
+    std::vector<uint32_t> order = light;
+    order.insert(order.end(), heavy.begin(), heavy.end());
+    const uint32_t n = (uint32_t)order.size();
+    if (!cuda_ok(cudaMemcpyAsync(s->order.p, order.data(), 4ull * n, cudaMemcpyHostToDevice, st),
                  "cudaMemcpyAsync") ||
-        !cuda_ok(cudaMemsetAsync(s->counters.p, 0, 16, st), "cudaMemsetAsync"))
+        !cuda_ok(cudaMemsetAsync(s->counters.p, 0, 32, st), "cudaMemsetAsync"))
         return GASTAR_CUDA_ERROR;
     LaunchParams P;
     std::memset(&P, 0, sizeof(P));
     P.insts = reinterpret_cast<const InstDesc*>(s->descs.p);
-    P.n_insts = n;
+    P.n_insts = (uint32_t)light.size();
     P.order = reinterpret_cast<const uint32_t*>(s->order.p);
     P.next = reinterpret_cast<uint32_t*>(s->counters.p);
     P.team_ctas = 1;
     P.slice_iters = s->cfg.slice_iters;
     P.barrier_timeout_ns = 2000000000ull;
-    const uint32_t blocks = std::min(n, s->max_active);
+    uint32_t blocks = std::min((uint32_t)light.size(), s->max_active);
+    if (!heavy.empty()) {
+        const uint32_t teams = std::min<uint32_t>(s->heavy_teams, (uint32_t)heavy.size());
+        P.heavy_order = reinterpret_cast<const uint32_t*>(s->order.p) + light.size();
+        P.n_heavy = (uint32_t)heavy.size();
+        P.heavy_team = s->cfg.heavy_team;
+        P.heavy_teams = teams;
+        P.heavy_next = reinterpret_cast<uint32_t*>(s->counters.p) + 4;
+        P.heavy_ctl = reinterpret_cast<TeamCtl*>(s->team_ctl.p);
+        P.heavy_stage = s->team_stage.p;
+        P.heavy_stage_bytes = s->heavy_stage_bytes;
+        blocks = std::max(blocks, teams * s->cfg.heavy_team);
+        if (!cuda_ok(cudaMemsetAsync(s->team_ctl.p, 0, sizeof(TeamCtl) * teams, st), "cudaMemsetAsync"))
+            return GASTAR_CUDA_ERROR;
+    }
     cudaEventRecord(s->e0, st);
     rc = launch_search(s->ctx, kKindsAll, P, blocks, s->threads, s->smem, st);
     if (rc != GASTAR_OK) return rc;

@@ -207,6 +207,9 @@ typedef struct gastar_serve_config {
     uint32_t heuristic, moves;
     uint32_t delta_grid;       /* pop window for grid requests (0 = none) */
     uint64_t sliding_states;   /* expected max states per puzzle request (0 = by size) */
+    uint32_t heavy_team;       /* blocks per team for heavy requests (1 = no teams) */
+    uint32_t heavy_teams;      /* teams per launch (0 = a quarter of the resident blocks) */
+    uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);
