@@ -47,6 +47,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(force: bool = False, verbose: bool = False, ptxas: bool = False) -> str:
     srcs = sources()
     if not force and not _stale(LIB, srcs + headers() + [__file__]):
+        if _stale(CLI, [os.path.join(HERE, "cli", "astar_gpu.cpp"), LIB]):
+            build_cli(verbose)
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
@@ -82,7 +84,23 @@ def build(force: bool = False, verbose: bool = False, ptxas: bool = False) -> st
         print(" ".join(link))
     subprocess.run(link, check=True)
     os.replace(tmp, LIB)
+    build_cli(verbose)
     return LIB
+
+
+CLI = os.path.join(BUILD, "astar_gpu")
+
+
+def build_cli(verbose: bool = False) -> str:
+    """The astar_gpu command (host C++ over the C ABI), next to the library."""
+    src = os.path.join(HERE, "cli", "astar_gpu.cpp")
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", CLI,
+           "-L", BUILD, "-lgastar", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return CLI
 
 
 if __name__ == "__main__":

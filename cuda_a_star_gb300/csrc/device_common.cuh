@@ -60,56 +60,68 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 
 // ---------------------------------------------------------------------------
-// Heap entries: 16 bytes for 64-bit state keys, 32 bytes for 128-bit keys.
+// Heap entries: a priority word and KW 64-bit key words (KW = 1..4), padded to
+// a multiple of 16 bytes: 16 B for 64-bit keys, 32 B for 128..192-bit keys,
+// 48 B for 256-bit keys.
 // ---------------------------------------------------------------------------
-template <int KW> struct Entry;
-template <> struct alignas(16) Entry<1> { uint64_t prio, k0; };
-template <> struct alignas(16) Entry<2> { uint64_t prio, k0, k1, pad; };
+template <int KW> struct alignas(16) Entry {
+    static constexpr int NK = KW + ((KW % 2 == 0) ? 1 : 0);  // key words incl. padding
+    uint64_t prio;
+    uint64_t k[NK];
+};
+template <int KW> __host__ __device__ constexpr int entry_vecs() { return (1 + Entry<KW>::NK) / 2; }
 
 template <int KW> __device__ __forceinline__ Entry<KW> inf_entry() {
     Entry<KW> e;
     e.prio = kInfPrio;
-    e.k0 = 0;
-    if constexpr (KW == 2) { e.k1 = 0; e.pad = 0; }
+#pragma unroll
+    for (int j = 0; j < Entry<KW>::NK; ++j) e.k[j] = 0;
     return e;
 }
 
 template <int KW> __device__ __forceinline__ Entry<KW> shfl_idx(const Entry<KW>& e, int src) {
     Entry<KW> r;
     r.prio = __shfl_sync(kFull, e.prio, src);
-    r.k0 = __shfl_sync(kFull, e.k0, src);
-    if constexpr (KW == 2) { r.k1 = __shfl_sync(kFull, e.k1, src); r.pad = 0; }
+#pragma unroll
+    for (int j = 0; j < Entry<KW>::NK; ++j) r.k[j] = j < KW ? __shfl_sync(kFull, e.k[j], src) : 0;
     return r;
 }
 
 template <int KW> __device__ __forceinline__ Entry<KW> shfl_xor(const Entry<KW>& e, int m) {
     Entry<KW> r;
     r.prio = __shfl_xor_sync(kFull, e.prio, m);
-    r.k0 = __shfl_xor_sync(kFull, e.k0, m);
-    if constexpr (KW == 2) { r.k1 = __shfl_xor_sync(kFull, e.k1, m); r.pad = 0; }
+#pragma unroll
+    for (int j = 0; j < Entry<KW>::NK; ++j) r.k[j] = j < KW ? __shfl_xor_sync(kFull, e.k[j], m) : 0;
     return r;
+}
+
+template <int KW> __device__ __forceinline__ void set_word(Entry<KW>& e, int w, uint64_t v) {
+    if (w == 0) e.prio = v;
+    else e.k[w - 1] = v;
+}
+template <int KW> __device__ __forceinline__ uint64_t get_word(const Entry<KW>& e, int w) {
+    return w == 0 ? e.prio : e.k[w - 1];
 }
 
 // L2-coherent loads/stores (heap nodes and stage buffers are handed between
 // launches and, in multi-block teams, between blocks).
 template <int KW> __device__ __forceinline__ Entry<KW> ld_entry(const Entry<KW>* p) {
     Entry<KW> e;
-    uint4 a = __ldcg(reinterpret_cast<const uint4*>(p));
-    e.prio = (uint64_t(a.y) << 32) | a.x;
-    e.k0 = (uint64_t(a.w) << 32) | a.z;
-    if constexpr (KW == 2) {
-        uint4 b = __ldcg(reinterpret_cast<const uint4*>(p) + 1);
-        e.k1 = (uint64_t(b.y) << 32) | b.x;
-        e.pad = 0;
+    const uint4* s = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int v = 0; v < entry_vecs<KW>(); ++v) {
+        const uint4 a = __ldcg(s + v);
+        set_word(e, 2 * v, (uint64_t(a.y) << 32) | a.x);
+        set_word(e, 2 * v + 1, (uint64_t(a.w) << 32) | a.z);
     }
     return e;
 }
 template <int KW> __device__ __forceinline__ void st_entry(Entry<KW>* p, const Entry<KW>& e) {
-    uint4 a = make_uint4(uint32_t(e.prio), uint32_t(e.prio >> 32), uint32_t(e.k0), uint32_t(e.k0 >> 32));
-    __stcg(reinterpret_cast<uint4*>(p), a);
-    if constexpr (KW == 2) {
-        uint4 b = make_uint4(uint32_t(e.k1), uint32_t(e.k1 >> 32), 0u, 0u);
-        __stcg(reinterpret_cast<uint4*>(p) + 1, b);
+    uint4* d = reinterpret_cast<uint4*>(p);
+#pragma unroll
+    for (int v = 0; v < entry_vecs<KW>(); ++v) {
+        const uint64_t a = get_word(e, 2 * v), b = get_word(e, 2 * v + 1);
+        __stcg(d + v, make_uint4(uint32_t(a), uint32_t(a >> 32), uint32_t(b), uint32_t(b >> 32)));
     }
 }
 
@@ -119,13 +131,12 @@ template <int KW> __device__ __forceinline__ void st_entry(Entry<KW>* p, const E
 template <int KW> __device__ __forceinline__ Entry<KW> ld_stage(const Entry<KW>* p, bool global) {
     if (global) return ld_entry(p);
     Entry<KW> e;
-    const uint4 a = *reinterpret_cast<const uint4*>(p);
-    e.prio = (uint64_t(a.y) << 32) | a.x;
-    e.k0 = (uint64_t(a.w) << 32) | a.z;
-    if constexpr (KW == 2) {
-        const uint4 b = *(reinterpret_cast<const uint4*>(p) + 1);
-        e.k1 = (uint64_t(b.y) << 32) | b.x;
-        e.pad = 0;
+    const uint4* s = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int v = 0; v < entry_vecs<KW>(); ++v) {
+        const uint4 a = s[v];
+        set_word(e, 2 * v, (uint64_t(a.y) << 32) | a.x);
+        set_word(e, 2 * v + 1, (uint64_t(a.w) << 32) | a.z);
     }
     return e;
 }
@@ -134,10 +145,12 @@ template <int KW> __device__ __forceinline__ void st_stage(Entry<KW>* p, const E
         st_entry(p, e);
         return;
     }
-    *reinterpret_cast<uint4*>(p) =
-        make_uint4(uint32_t(e.prio), uint32_t(e.prio >> 32), uint32_t(e.k0), uint32_t(e.k0 >> 32));
-    if constexpr (KW == 2)
-        *(reinterpret_cast<uint4*>(p) + 1) = make_uint4(uint32_t(e.k1), uint32_t(e.k1 >> 32), 0u, 0u);
+    uint4* d = reinterpret_cast<uint4*>(p);
+#pragma unroll
+    for (int v = 0; v < entry_vecs<KW>(); ++v) {
+        const uint64_t a = get_word(e, 2 * v), b = get_word(e, 2 * v + 1);
+        d[v] = make_uint4(uint32_t(a), uint32_t(a >> 32), uint32_t(b), uint32_t(b >> 32));
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -11,7 +11,7 @@
 namespace gastar {
 
 // Problem kinds compiled into the search kernel.
-enum Kind : uint32_t { KIND_SLIDING3 = 0, KIND_SLIDING4 = 1, KIND_SLIDING5 = 2, KIND_GRID = 3 };
+enum Kind : uint32_t { KIND_SLIDING3 = 0, KIND_SLIDING4 = 1, KIND_SLIDING5 = 2, KIND_GRID = 3, KIND_PLUGIN = 4 };
 constexpr uint32_t kKindsAll = 0xf;
 constexpr uint32_t kind_bit(uint32_t k) { return 1u << k; }
 
@@ -62,6 +62,7 @@ struct alignas(16) InstDesc {
     unsigned long long* touched_count;
     uint64_t touched_cap;
     uint32_t prev_slot_words, pad1;
+    uint64_t start_hi[2], goal_hi[2];  // key words 2..3 (generic plugin states)
 };
 
 // Per-iteration team state; iteration t uses slot t % kSlots.

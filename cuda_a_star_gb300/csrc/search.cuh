@@ -50,12 +50,12 @@ template <int N> struct SlidingDom {
         return uint32_t(k >> (B * i)) & ((1u << B) - 1);
     }
     static __device__ __forceinline__ KeyT key_of(const Entry<KW>& e) {
-        if constexpr (KW == 1) return e.k0;
-        else return (KeyT(e.k1) << 64) | KeyT(e.k0);
+        if constexpr (KW == 1) return e.k[0];
+        else return (KeyT(e.k[1]) << 64) | KeyT(e.k[0]);
     }
     static __device__ __forceinline__ void set_key(Entry<KW>& e, KeyT k) {
-        e.k0 = uint64_t(k);
-        if constexpr (KW == 2) e.k1 = uint64_t(k >> 64);
+        e.k[0] = uint64_t(k);
+        if constexpr (KW == 2) e.k[1] = uint64_t(k >> 64);
     }
     static __device__ __forceinline__ KeyT desc_key(uint64_t lo, uint64_t hi) {
         if constexpr (KW == 1) return lo;
@@ -112,6 +112,11 @@ template <int N> struct SlidingDom {
         if constexpr (KW == 1) return tab_get(t, k);
         else return tab_get(t, uint64_t(k), uint64_t(k >> 64));
     }
+    static __device__ __forceinline__ uint32_t start_f(const Ctx&, const InstDesc& d) { return d.f0; }
+    // Parents are recorded by move code; the root's code is kRootMove.
+    static constexpr uint32_t kRootCode = kRootMove;
+    static __device__ __forceinline__ uint64_t get_self(const Tab& t, KeyT k, uint32_t&) { return get(t, k); }
+    static __device__ __forceinline__ uint32_t code(int m, uint32_t) { return (uint32_t)m; }
     static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
                                                  uint64_t& slot) {
         if constexpr (KW == 1) return tab_insert(t, k, v, old, slot);
@@ -161,7 +166,7 @@ template <int N> struct SlidingDom {
     }
 
     // Parent of k when k was reached with move m: the blank moves back.
-    static __device__ __forceinline__ KeyT parent(const Ctx&, KeyT k, uint32_t m) {
+    static __device__ __forceinline__ KeyT parent(const Ctx&, const Tab&, KeyT k, uint32_t m) {
         const int p = blank_of(k);
         const int q = (m == 0) ? p - N : (m == 1) ? p + N : (m == 2) ? p - 1 : p + 1;
         const uint32_t t = field(k, q);
@@ -191,8 +196,8 @@ struct GridDom {
     static __device__ __forceinline__ int dy(int m) { return (m == 2 || m == 4 || m == 6) ? 1 : (m == 3 || m == 5 || m == 7) ? -1 : 0; }
     static __device__ __forceinline__ uint32_t inv(uint32_t m) { return m < 4 ? (m ^ 1) : 11 - m; }
 
-    static __device__ __forceinline__ KeyT key_of(const Entry<1>& e) { return e.k0; }
-    static __device__ __forceinline__ void set_key(Entry<1>& e, KeyT k) { e.k0 = k; }
+    static __device__ __forceinline__ KeyT key_of(const Entry<1>& e) { return e.k[0]; }
+    static __device__ __forceinline__ void set_key(Entry<1>& e, KeyT k) { e.k[0] = k; }
 
     static __device__ void load(Ctx& c, const InstDesc& d) {
         if (threadIdx.x == 0) {
@@ -210,6 +215,10 @@ struct GridDom {
     }
     static __device__ __forceinline__ Tab make_tab(const InstDesc& d) { return Tab{d.table}; }
     static __device__ __forceinline__ uint64_t get(const Tab& t, KeyT k) { return __ldcg(t.v + k); }
+    static __device__ __forceinline__ uint32_t start_f(const Ctx&, const InstDesc& d) { return d.f0; }
+    static constexpr uint32_t kRootCode = kRootMove;
+    static __device__ __forceinline__ uint64_t get_self(const Tab& t, KeyT k, uint32_t&) { return get(t, k); }
+    static __device__ __forceinline__ uint32_t code(int m, uint32_t) { return (uint32_t)m; }
     static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
                                                  uint64_t& slot) {
         old = atomicMin(t.v + k, v);
@@ -253,7 +262,7 @@ struct GridDom {
         nh = heur(c, nx, ny);
         return true;
     }
-    static __device__ __forceinline__ KeyT parent(const Ctx& c, KeyT k, uint32_t m) {
+    static __device__ __forceinline__ KeyT parent(const Ctx& c, const Tab&, KeyT k, uint32_t m) {
         return (KeyT)((int64_t)k - dx((int)m) - (int64_t)dy((int)m) * (int64_t)c.W);
     }
 };
@@ -416,14 +425,14 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         if (!tsync()) status = ST_BARRIER;
         if (hid == 0) {
             E s = inf_entry<KW>();
-            s.prio = make_prio(d.f0, 0);
+            s.prio = make_prio(D::start_f(ctx, d), 0);
             D::set_key(s, ctx.start);
             if (lane == 0) hp.part = s;
             hp.pc = 1;
         }
         if (leader) {
             uint64_t old, slot = 0;
-            D::insert(tab, ctx.start, make_val(0, kRootMove), old, slot);
+            D::insert(tab, ctx.start, make_val(0, D::kRootCode), old, slot);
             if (d.touched) {
                 *d.touched_count = 1;
                 d.touched[0] = (uint32_t)slot;
@@ -441,7 +450,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     if (status == kInf && !tsync()) status = ST_BARRIER;
 
     const uint32_t ew = d.ew;
-    uint32_t fmin = d.f0;  // min f over the open list at the last check
+    uint32_t fmin = D::start_f(ctx, d);  // min f over the open list at the last check
     uint32_t it = 0;
     const uint32_t it0 = ld_vol(&ctl->iterations);
     while (status == kInf) {
@@ -476,16 +485,16 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
-        uint32_t pm = kRootMove;
+        uint32_t pm = D::kRootCode, self = 0;
         bool stale = false;
         uint32_t goal_g = kInf;
         if (act) {
-            const uint64_t v = D::get(tab, k);
+            const uint64_t v = D::get_self(tab, k, self);
             if ((uint32_t)(v >> 32) < g) {
                 stale = true;
                 act = false;
             } else {
-                pm = (uint32_t)v & 0xffu;
+                pm = (uint32_t)v;
             }
         }
         if (act && D::is_goal(ctx, k)) {
@@ -524,7 +533,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             uint64_t old[GS];
 #pragma unroll
             for (int j = 0; j < GS; ++j)
-                old[j] = (ok[j] && cl[j] >= 0) ? D::min_at(tab, slot[j], make_val(ng[j], (uint32_t)(g0 + j)))
+                old[j] = (ok[j] && cl[j] >= 0) ? D::min_at(tab, slot[j], make_val(ng[j], D::code(g0 + j, self)))
                                                : 0ull;
             uint32_t nacc = 0, ncl = 0;
             bool acc[GS], clm[GS];
@@ -760,13 +769,13 @@ __device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long
     uint64_t len = 1;
     for (typename D::KeyT k = ctx.goal; !D::is_start(ctx, k); ++len) {
         const uint64_t v = D::get(tab, k);
-        const uint32_t m = (uint32_t)v & 0xffu;
-        if (v == kEmpty || m == kRootMove || len > limit) {
+        const uint32_t m = (uint32_t)v;
+        if (v == kEmpty || m == D::kRootCode || len > limit) {
             ctl->status = ST_PATH_CAP;
             ctl->path_len = 0;
             return;
         }
-        k = D::parent(ctx, k, m);
+        k = D::parent(ctx, tab, k, m);
     }
     const unsigned long long words = len * D::KW;
     const unsigned long long off = atomicAdd(arena_used, words);
@@ -781,7 +790,7 @@ __device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long
         unsigned long long* o = arena + off + i * D::KW;
         o[0] = (uint64_t)k;
         if constexpr (D::KW == 2) o[1] = (uint64_t)(k >> 64);
-        if (i + 1 < len) k = D::parent(ctx, k, (uint32_t)D::get(tab, k) & 0xffu);
+        if (i + 1 < len) k = D::parent(ctx, tab, k, (uint32_t)D::get(tab, k));
     }
 }
 
