@@ -24,7 +24,8 @@ H_ADMISSIBLE, H_REFERENCE, H_ZERO = 0, 1, 2
 MOVES_STANDARD, MOVES_REFERENCE = 0, 1
 
 STATUS = ["OK", "NO_PATH", "BUDGET", "TIMEOUT", "HEAP_FULL", "TABLE_FULL", "PATH_CAP",
-          "BARRIER_TIMEOUT", "BAD_INPUT", "CUDA_ERROR", "NO_DEVICE", "PENDING", "OUT_OF_MEMORY"]
+          "BARRIER_TIMEOUT", "BAD_INPUT", "CUDA_ERROR", "NO_DEVICE", "PENDING", "OUT_OF_MEMORY",
+          "COST_RANGE"]
 OK, NO_PATH = 0, 1
 
 

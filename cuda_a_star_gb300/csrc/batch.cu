@@ -281,7 +281,7 @@ int batch_upload(gastar_batch* b) {
     b->n_sched = (uint32_t)order.size();
     order.insert(order.end(), horder.begin(), horder.end());
     if (b->n_heavy) {
-        b->heavy_stage_bytes = 2 * stage_entries_per_buffer(pch.warps, pch.ew, 8) * 16;
+        b->heavy_stage_bytes = team_stage_bytes(T, pc.warps, pc.ew, 8, 16);
         if (!b->team_ctl.ensure(sizeof(TeamCtl) * b->heavy_teams) ||
             !b->team_stage.ensure(b->heavy_stage_bytes * b->heavy_teams))
             return GASTAR_OUT_OF_MEMORY;

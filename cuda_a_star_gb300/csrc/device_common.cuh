@@ -24,7 +24,7 @@ constexpr uint32_t kRootMove = 0xffu;   // parent move of the start state
 // Device status codes; the numeric values are the gastar_status values of the C ABI.
 enum : uint32_t {
     ST_OK = 0, ST_NO_PATH = 1, ST_BUDGET = 2, ST_TIMEOUT = 3, ST_HEAP_FULL = 4,
-    ST_TABLE_FULL = 5, ST_PATH_CAP = 6, ST_BARRIER = 7, ST_BAD_INPUT = 8,
+    ST_TABLE_FULL = 5, ST_PATH_CAP = 6, ST_BARRIER = 7, ST_BAD_INPUT = 8, ST_COST_RANGE = 13,
 };
 enum : uint32_t { LIFE_FRESH = 0, LIFE_RUNNING = 1, LIFE_DONE = 2 };
 
@@ -38,14 +38,18 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
     return x;
 }
 
-// Priority word: f in the high half, (2^32-1 - g) in the low half, so that
-// one unsigned comparison gives the reference's order "lower f first, equal
-// f -> higher g first" (QueueValue::operator<, a_star.h:58-63).
-__host__ __device__ __forceinline__ uint64_t make_prio(uint32_t f, uint32_t g) {
-    return (uint64_t(f) << 32) | uint64_t(0xffffffffu - g);
+// Priority word: f in bits 63..32, (2^24-1 - g) in bits 31..8 and the move
+// that produced the entry in bits 7..0, so that one unsigned comparison gives
+// the reference's order "lower f first, equal f -> higher g first"
+// (QueueValue::operator<, a_star.h:58-63) and a popped entry knows its parent
+// move without a table lookup.  Costs are limited to kMaxG.
+constexpr uint32_t kMaxG = 0xffffffu;
+__host__ __device__ __forceinline__ uint64_t make_prio(uint32_t f, uint32_t g, uint32_t pm = 0xffu) {
+    return (uint64_t(f) << 32) | (uint64_t(kMaxG - g) << 8) | (pm & 0xffu);
 }
 __host__ __device__ __forceinline__ uint32_t prio_f(uint64_t p) { return uint32_t(p >> 32); }
-__host__ __device__ __forceinline__ uint32_t prio_g(uint64_t p) { return 0xffffffffu - uint32_t(p); }
+__host__ __device__ __forceinline__ uint32_t prio_g(uint64_t p) { return kMaxG - (uint32_t(p >> 8) & kMaxG); }
+__host__ __device__ __forceinline__ uint32_t prio_pm(uint64_t p) { return uint32_t(p) & 0xffu; }
 
 // Table value word: g in the high half, parent move in the low byte; one
 // 64-bit atomicMin keeps the lowest g and, among equal g, the lowest move.
@@ -212,20 +216,20 @@ __device__ __forceinline__ Entry<KW> pick(const Entry<KW>& lo, const Entry<KW>& 
 // order is node-wise (every entry of a node <= every entry of its children),
 // so the root holds the 32 best entries of the tree.  The root node and a
 // partial buffer of < 32 entries live in registers (one entry per lane) for
-// the lifetime of a launch, nodes 1..kHeapSmemNodes-1 in shared memory, the
-// rest are 512-byte (or 1 KiB) blocks in global memory read and written with
+// the lifetime of a launch, nodes 1..sn-1 in shared memory (the top levels;
+// sn is chosen per launch from the shared memory left on the SM), the rest are 512-byte (or 1 KiB) blocks in global memory read and written with
 // one coalesced access per lane.  Replaces the reference's one-thread-per-heap
 // binary heaps with their key->slot index (heaps.h:93-177, device_hashmap.h):
 // stale entries are dropped at pop time instead of being erased (lazy
 // deletion).
 // ---------------------------------------------------------------------------
-constexpr uint32_t kHeapSmemNodes = 7;  // nodes 1..6 staged in shared memory
 
 template <int KW> struct WarpHeap {
     Entry<KW>* nodes;   // (cap + 1) * 32 entries; node `cap` stores the saved partial buffer
-    Entry<KW>* snodes;  // shared memory: nodes 1..kHeapSmemNodes-1
+    Entry<KW>* snodes;  // shared memory: nodes 1..sn-1
     uint32_t* hdr;      // saved {N, pc}
-    uint32_t cap;       // tree nodes available (>= kHeapSmemNodes)
+    uint32_t cap;       // tree nodes available (>= sn)
+    uint32_t sn;        // nodes below sn live in shared memory (node 0 in registers)
     uint32_t N;         // full nodes in the tree (warp-uniform)
     uint32_t pc;        // entries in the partial buffer (warp-uniform)
     uint32_t max_n;     // high-water mark of N
@@ -235,17 +239,17 @@ template <int KW> struct WarpHeap {
 
 template <int KW>
 __device__ __forceinline__ Entry<KW> ld_node(const WarpHeap<KW>& h, uint32_t idx, int lane) {
-    if (idx < kHeapSmemNodes) return ld_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, false);
+    if (idx < h.sn) return ld_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, false);
     return ld_entry(h.nodes + (size_t)idx * 32 + lane);
 }
 template <int KW>
 __device__ __forceinline__ void st_node(const WarpHeap<KW>& h, uint32_t idx, int lane, const Entry<KW>& e) {
-    if (idx < kHeapSmemNodes) st_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, e, false);
+    if (idx < h.sn) st_stage(h.snodes + (size_t)(idx - 1) * 32 + lane, e, false);
     else st_entry(h.nodes + (size_t)idx * 32 + lane, e);
 }
 // Priority of the largest entry of node idx (one read, broadcast to the warp).
 template <int KW> __device__ __forceinline__ uint64_t node_max(const WarpHeap<KW>& h, uint32_t idx) {
-    if (idx < kHeapSmemNodes) return *reinterpret_cast<const volatile uint64_t*>(&h.snodes[(size_t)(idx - 1) * 32 + 31].prio);
+    if (idx < h.sn) return *reinterpret_cast<const volatile uint64_t*>(&h.snodes[(size_t)(idx - 1) * 32 + 31].prio);
     return __ldcg(reinterpret_cast<const unsigned long long*>(&h.nodes[(size_t)idx * 32 + 31].prio));
 }
 
@@ -263,7 +267,7 @@ template <int KW> __device__ __forceinline__ void heap_restore(WarpHeap<KW>& h, 
     h.max_n = h.N;
     h.root = h.N ? ld_entry(h.nodes + lane) : inf_entry<KW>();
     h.part = (uint32_t)lane < h.pc ? ld_entry(h.nodes + (size_t)h.cap * 32 + lane) : inf_entry<KW>();
-    for (uint32_t i = 1; i < h.N && i < kHeapSmemNodes; ++i)
+    for (uint32_t i = 1; i < h.N && i < h.sn; ++i)
         st_stage(h.snodes + (size_t)(i - 1) * 32 + lane, ld_entry(h.nodes + (size_t)i * 32 + lane), false);
     __syncwarp();
 }
@@ -271,7 +275,7 @@ template <int KW> __device__ __forceinline__ void heap_restore(WarpHeap<KW>& h, 
 template <int KW> __device__ __forceinline__ void heap_save(const WarpHeap<KW>& h, int lane) {
     __syncwarp();
     if (h.N) st_entry(h.nodes + lane, h.root);
-    for (uint32_t i = 1; i < h.N && i < kHeapSmemNodes; ++i)
+    for (uint32_t i = 1; i < h.N && i < h.sn; ++i)
         st_entry(h.nodes + (size_t)i * 32 + lane, ld_stage(h.snodes + (size_t)(i - 1) * 32 + lane, false));
     st_entry(h.nodes + (size_t)h.cap * 32 + lane, h.part);
     if (lane == 0) {
@@ -455,37 +459,103 @@ __device__ bool heap_push(WarpHeap<KW>& h, Entry<KW> x, uint32_t m, int lane) {
 // (fancy_hashmap.h:32-81, 155-167) as one atomic per successor.
 // ---------------------------------------------------------------------------
 
-// 64-bit keys: slot = {key, value}, 16 bytes; linear probing.
+// Claim protocol shared by the tables.  claim_first / claim_probe return
+//   -1 full, 2 home slot taken by another key (claim_probe walks on),
+//   0 found / 1 claimed, with `old` the value word before this update (done),
+//   4 found / 5 claimed, with the value still to be lowered by min_at.
+constexpr int kClNeedMin = 4;
+
+__device__ __forceinline__ void cas128(unsigned long long* addr, uint64_t c0, uint64_t c1,
+                                       uint64_t n0, uint64_t n1, uint64_t& o0, uint64_t& o1) {
+    asm volatile(
+        "{\n\t.reg .b128 cmp, swp, dst;\n\t"
+        "mov.b128 cmp, {%2, %3};\n\t"
+        "mov.b128 swp, {%4, %5};\n\t"
+        "atom.global.cas.b128 dst, [%6], cmp, swp;\n\t"
+        "mov.b128 {%0, %1}, dst;\n\t}"
+        : "=l"(o0), "=l"(o1)
+        : "l"(c0), "l"(c1), "l"(n0), "l"(n1), "l"(addr)
+        : "memory");
+}
+
+// 64-bit keys: slot = {key, value}, 16 bytes; linear probing.  Every atomic
+// on a slot is one 16-byte compare-and-swap of the pair: a new key is claimed
+// with its value in one round trip, a known key costs none more unless its
+// value drops.
 struct HashTab64 {
     unsigned long long* s;
     uint64_t mask;
     uint32_t max_probe;
 };
 
-// Returns 1 when the key was newly claimed, 0 when found, -1 when full;
-// `slot` receives the slot's first word offset.
-__device__ __forceinline__ int tab_insert(const HashTab64& t, uint64_t key, uint64_t val,
-                                          uint64_t& old, uint64_t& slot) {
-    uint64_t i = mix64(key) & t.mask;
-    for (uint32_t p = 0; p < t.max_probe; ++p) {
-        unsigned long long* ks = t.s + 2 * i;
-        unsigned long long k = __ldcg(ks);
-        int claimed = 0;
-        if (k == kEmpty) {
-            k = atomicCAS(ks, kEmpty, key);
-            if (k == kEmpty) {
-                k = key;
-                claimed = 1;
-            }
-        }
-        if (k == key) {
-            old = atomicMin(ks + 1, val);
-            slot = 2 * i;
-            return claimed;
-        }
+__device__ __forceinline__ int tab_claim_at(const HashTab64& t, uint64_t i, uint64_t key, uint64_t val,
+                                            uint64_t& old) {
+    uint64_t o0, o1;
+    cas128(t.s + 2 * i, kEmpty, kEmpty, key, val, o0, o1);
+    if (o0 == kEmpty && o1 == kEmpty) {
+        old = kEmpty;
+        return 1;
+    }
+    if (o0 != key) return 2;
+    old = o1;
+    return o1 > val ? kClNeedMin : 0;
+}
+__device__ __forceinline__ int tab_claim_first(const HashTab64& t, uint64_t key, uint64_t val, uint64_t& slot,
+                                               uint64_t& old) {
+    const uint64_t i = mix64(key) & t.mask;
+    slot = 2 * i;
+    return tab_claim_at(t, i, key, val, old);
+}
+__device__ __forceinline__ int tab_claim_probe(const HashTab64& t, uint64_t key, uint64_t val, uint64_t& slot,
+                                               uint64_t& old) {
+    uint64_t i = slot / 2;
+    for (uint32_t p = 1; p < t.max_probe; ++p) {
         i = (i + 1) & t.mask;
+        const int r = tab_claim_at(t, i, key, val, old);
+        if (r != 2) {
+            slot = 2 * i;
+            return r;
+        }
     }
     return -1;
+}
+// Lowers the value of a found key to `val` unless it is already <= val;
+// `seen` is the value the claim read.  Returns the value before the update.
+// Values only fall, so every failed exchange is followed by a strictly lower
+// value; the retry bound is far beyond the number of concurrent updaters.
+__device__ __forceinline__ uint64_t tab_min_at(const HashTab64& t, uint64_t slot, uint64_t key, uint64_t val,
+                                               uint64_t seen) {
+    uint64_t cur = seen;
+    for (uint32_t r = 0; cur > val && r < 4096; ++r) {
+        uint64_t o0, o1;
+        cas128(t.s + slot, key, cur, key, val, o0, o1);
+        if (o1 == cur) break;
+        cur = o1;
+    }
+    return cur;
+}
+// Returns 1 when the key was newly claimed, 0 when found, -1 when full.
+__device__ __forceinline__ int tab_insert(const HashTab64& t, uint64_t key, uint64_t val, uint64_t& old,
+                                          uint64_t& slot) {
+    int r = tab_claim_first(t, key, val, slot, old);
+    if (r == 2) r = tab_claim_probe(t, key, val, slot, old);
+    if (r == kClNeedMin) {
+        old = tab_min_at(t, slot, key, val, old);
+        r = 0;
+    }
+    return r;
+}
+
+// Two-step lookup: look_begin issues the home-slot load, look_end resolves
+// it (probing on when the home slot holds another key), so the load can be in
+// flight while other memory work is issued.
+struct Look64 {
+    unsigned long long k, v;
+};
+__device__ __forceinline__ Look64 tab_look_begin(const HashTab64& t, uint64_t key) {
+    const uint64_t i = mix64(key) & t.mask;
+    const ulonglong2 kv = __ldcg(reinterpret_cast<const ulonglong2*>(t.s + 2 * i));
+    return Look64{kv.x, kv.y};
 }
 
 __device__ __forceinline__ uint64_t tab_get(const HashTab64& t, uint64_t key) {
@@ -508,19 +578,6 @@ struct HashTab128 {
     uint64_t mask;
     uint32_t max_probe;
 };
-
-__device__ __forceinline__ void cas128(unsigned long long* addr, uint64_t c0, uint64_t c1,
-                                       uint64_t n0, uint64_t n1, uint64_t& o0, uint64_t& o1) {
-    asm volatile(
-        "{\n\t.reg .b128 cmp, swp, dst;\n\t"
-        "mov.b128 cmp, {%2, %3};\n\t"
-        "mov.b128 swp, {%4, %5};\n\t"
-        "atom.global.cas.b128 dst, [%6], cmp, swp;\n\t"
-        "mov.b128 {%0, %1}, dst;\n\t}"
-        : "=l"(o0), "=l"(o1)
-        : "l"(c0), "l"(c1), "l"(n0), "l"(n1), "l"(addr)
-        : "memory");
-}
 
 __device__ __forceinline__ uint64_t hash128(uint64_t k0, uint64_t k1) {
     return mix64(k0 ^ mix64(k1 + 0x9e3779b97f4a7c15ull));
@@ -562,49 +619,15 @@ struct DenseTab {
     unsigned long long* v;
 };
 
-// Two-step insert-or-min used by the expansion loop, so that the probes of all
-// successors of a lane are in flight together: claim_first issues one CAS at
-// the home slot (1 = claimed, 0 = found, 2 = occupied by another key),
-// claim_probe walks on from there (-1 = full), min_at applies the atomicMin
-// to the value word and returns the old value.
-__device__ __forceinline__ int tab_claim_first(const HashTab64& t, uint64_t key, uint64_t& slot) {
-    const uint64_t i = mix64(key) & t.mask;
-    slot = 2 * i;
-    const unsigned long long k = atomicCAS(t.s + 2 * i, kEmpty, key);
-    return k == kEmpty ? 1 : (k == key ? 0 : 2);
-}
-__device__ __forceinline__ int tab_claim_probe(const HashTab64& t, uint64_t key, uint64_t& slot) {
-    uint64_t i = slot / 2;
-    for (uint32_t p = 1; p < t.max_probe; ++p) {
-        i = (i + 1) & t.mask;
-        unsigned long long* ks = t.s + 2 * i;
-        unsigned long long k = __ldcg(ks);
-        int claimed = 0;
-        if (k == kEmpty) {
-            k = atomicCAS(ks, kEmpty, key);
-            if (k == kEmpty) {
-                k = key;
-                claimed = 1;
-            }
-        }
-        if (k == key) {
-            slot = 2 * i;
-            return claimed;
-        }
-    }
-    return -1;
-}
-__device__ __forceinline__ uint64_t tab_min_at(const HashTab64& t, uint64_t slot, uint64_t val) {
-    return atomicMin(t.s + slot + 1, val);
-}
-
+// 128-bit keys: the key pair is claimed with a 16-byte compare-and-swap, the
+// value word beside it is lowered with atomicMin.
 __device__ __forceinline__ int tab_claim_first(const HashTab128& t, uint64_t k0, uint64_t k1, uint64_t& slot) {
     const uint64_t i = hash128(k0, k1) & t.mask;
     slot = 4 * i;
     uint64_t o0, o1;
     cas128(t.s + 4 * i, kEmpty, kEmpty, k0, k1, o0, o1);
-    if (o0 == kEmpty && o1 == kEmpty) return 1;
-    return (o0 == k0 && o1 == k1) ? 0 : 2;
+    if (o0 == kEmpty && o1 == kEmpty) return kClNeedMin | 1;
+    return (o0 == k0 && o1 == k1) ? kClNeedMin : 2;
 }
 __device__ __forceinline__ int tab_claim_probe(const HashTab128& t, uint64_t k0, uint64_t k1, uint64_t& slot) {
     uint64_t i = slot / 4;
@@ -615,7 +638,7 @@ __device__ __forceinline__ int tab_claim_probe(const HashTab128& t, uint64_t k0,
         const int claimed = (o0 == kEmpty && o1 == kEmpty);
         if (claimed || (o0 == k0 && o1 == k1)) {
             slot = 4 * i;
-            return claimed;
+            return kClNeedMin | claimed;
         }
     }
     return -1;

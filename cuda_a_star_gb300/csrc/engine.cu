@@ -73,13 +73,13 @@ uint32_t entry_bytes(uint32_t kind) { return kind == KIND_SLIDING5 ? 32u : 16u; 
 uint32_t max_neighbours(uint32_t kind) { return kind == KIND_GRID ? 8u : 4u; }
 uint32_t key_words(uint32_t kind) { return kind == KIND_SLIDING5 ? 2u : 1u; }
 
-size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi) {
+size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t heap_snodes) {
     // Two stage buffers (one-block teams) + shared-memory heap nodes per warp.
     size_t best = 0;
     for (uint32_t k = 0; k < 4; ++k)
         if (kinds & kind_bit(k)) {
             const size_t stage = multi ? 0 : 2 * stage_entries_per_buffer(warps, ew, max_neighbours(k)) * entry_bytes(k);
-            best = std::max(best, stage + (size_t)warps * (kHeapSmemNodes - 1) * 32 * entry_bytes(k));
+            best = std::max(best, stage + (size_t)warps * (heap_snodes - 1) * 32 * entry_bytes(k));
         }
     return best;
 }
@@ -216,7 +216,7 @@ const char* gastar_last_error(void) { return g_last_error.c_str(); }
 const char* gastar_status_name(int s) {
     static const char* names[] = {"OK", "NO_PATH", "BUDGET", "TIMEOUT", "HEAP_FULL", "TABLE_FULL",
                                   "PATH_CAP", "BARRIER_TIMEOUT", "BAD_INPUT", "CUDA_ERROR",
-                                  "NO_DEVICE", "PENDING", "OUT_OF_MEMORY"};
+                                  "NO_DEVICE", "PENDING", "OUT_OF_MEMORY", "COST_RANGE"};
     if (s < 0 || s >= (int)(sizeof(names) / sizeof(names[0]))) return "UNKNOWN";
     return names[s];
 }
@@ -255,6 +255,8 @@ gastar_ctx* gastar_create(int device) {
     c->mem_total = prop.totalGlobalMem;
     std::snprintf(c->name, sizeof(c->name), "%s", prop.name);
     c->coop = prop.cooperativeLaunch;
+    c->smem_per_sm = prop.sharedMemPerMultiprocessor;
+    c->smem_optin = prop.sharedMemPerBlockOptin;
     if (!cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreate(&c->e0), "cudaEventCreate") ||
         !cuda_ok(cudaEventCreate(&c->e1), "cudaEventCreate") ||
@@ -327,18 +329,39 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
                          cudaStream_t st, InstCtl& ctl_out, AttemptStats& as) {
     const uint32_t kinds = kind_bit(pp.kind);
     const uint32_t ew = std::min(32u, std::max(1u, cfg.expansion_width ? cfg.expansion_width : 32u));
-    const uint32_t W = std::min(16u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
+    const uint32_t W = std::min(8u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
     const uint32_t threads = W * 32;
     const uint64_t Q = cfg.num_queues ? cfg.num_queues : 4096;
     uint64_t heaps = (Q + ew - 1) / ew;
     uint64_t blocks = (heaps + W - 1) / W;
     const bool multi = blocks > 1;
-    const size_t smem = block_smem_bytes(kinds, W, ew, multi);
+    size_t smem = block_smem_bytes(kinds, W, ew, multi);
     const int nb = occupancy_blocks(c, kinds, threads, smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
     uint64_t max_blocks = (uint64_t)nb * c->sms;
     if (cfg.max_blocks) max_blocks = std::min<uint64_t>(max_blocks, cfg.max_blocks);
     if (blocks > max_blocks) blocks = max_blocks;
+    // The heaps' top levels go to the shared memory the co-resident blocks
+    // leave free: pops and pushes then touch global nodes only deep down.
+    uint32_t snodes = kHeapSmemNodes;
+    {
+        const uint64_t per_sm = (blocks + c->sms - 1) / c->sms;
+        const size_t base = block_smem_bytes(kinds, W, ew, multi, 1);
+        const size_t node = (size_t)W * 32 * entry_bytes(pp.kind);
+        const size_t reserve = 4096;  // static shared memory + per-block system share
+        size_t budget = c->smem_per_sm / per_sm;
+        budget = budget > reserve ? std::min(budget - reserve, c->smem_optin) : 0;
+        if (budget > base + (kHeapSmemNodes - 1) * node) {
+            const uint64_t n = 1 + (budget - base) / node;
+            const uint32_t cand = (uint32_t)std::min<uint64_t>(n, kHeapSmemNodesMax);
+            const size_t s2 = block_smem_bytes(kinds, W, ew, multi, cand);
+            const int nb2 = occupancy_blocks(c, kinds, threads, s2);
+            if (nb2 > 0 && (uint64_t)nb2 * c->sms >= blocks) {
+                snodes = cand;
+                smem = s2;
+            }
+        }
+    }
     if (multi && !c->coop) {
         set_error("device does not support cooperative launch");
         return GASTAR_CUDA_ERROR;
@@ -364,7 +387,9 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         float lf = cfg.load_factor > 0.f ? cfg.load_factor : 0.75f;
         lf = std::min(0.95f, std::max(0.1f, lf));
         limit = (uint64_t)((double)slots * lf);
-        touched_cap = limit + heaps * ew * maxn + 16;
+        // Claims stop within two iterations past the limit; every warp may
+        // leave one chunk partly unused.
+        touched_cap = limit + 2 * heaps * ew * maxn + heaps * kTouchedChunk + 16;
         tb = &c->table;
         // A reallocated table, claim list or claim counter loses the record of
         // what the previous solve wrote: clear the whole table then.
@@ -384,13 +409,13 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     }
     // Heaps: per warp-heap node capacity with headroom for uneven dealing.
     uint64_t per_heap = (heap_entries + heaps - 1) / heaps;
-    uint64_t cap_nodes = std::max<uint64_t>(2 * kHeapSmemNodes, (per_heap * 2 + 31) / 32);
+    uint64_t cap_nodes = std::max<uint64_t>(2 * snodes, (per_heap * 2 + 31) / 32);
     if (cap_nodes > 0x7fffffffull) return GASTAR_OUT_OF_MEMORY;
     const size_t heap_bytes = (size_t)heaps * (cap_nodes + 1) * 32 * ebytes;
-    const size_t stage_entries = multi ? 2 * stage_entries_per_buffer(heaps, ew, maxn) : 0;
+    const size_t stage_bytes = multi ? team_stage_bytes((uint32_t)blocks, W, ew, maxn, ebytes) : 16;
 
     if (!c->heaps.ensure(heap_bytes) || !c->hdr.ensure((size_t)heaps * 8) ||
-        !c->stage.ensure(std::max<size_t>(stage_entries * ebytes, 16)) ||
+        !c->stage.ensure(stage_bytes) ||
         !c->desc.ensure(sizeof(InstDesc)) || !c->ctl.ensure(sizeof(InstCtl)) ||
         !c->team.ensure(sizeof(TeamCtl) + 64))
         return GASTAR_OUT_OF_MEMORY;
@@ -448,6 +473,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     P.n_insts = 1;
     P.next = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(c->team.p) + sizeof(TeamCtl));
     P.team_ctas = (uint32_t)blocks;
+    P.heap_snodes = snodes;
     P.team = reinterpret_cast<TeamCtl*>(c->team.p);
     P.stage = c->stage.p;
     P.barrier_timeout_ns = 2000000000ull;
@@ -467,7 +493,9 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     as.d2h += sizeof(InstCtl);
     if (pp.kind != KIND_GRID) {
         c->prev_slot_words = slot_words;
-        if (c->h_ctl->table_used > touched_cap) c->table_dirty = true;  // claim list overflowed
+        // Reserved entries <= 1 + claims + one chunk per warp: beyond the
+        // list's size some claims went unrecorded.
+        if (1 + c->h_ctl->table_used + heaps * kTouchedChunk > touched_cap) c->table_dirty = true;
     }
     if (want_path && c->h_ctl->status == ST_OK) {
         // best + 1 states is the longest possible path (every step costs >= 1).

@@ -27,7 +27,8 @@ const void* search_kernel_for(uint32_t kinds);
 uint32_t entry_bytes(uint32_t kind);
 uint32_t max_neighbours(uint32_t kind);
 uint32_t key_words(uint32_t kind);
-size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi);
+size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi,
+                        uint32_t heap_snodes = kHeapSmemNodes);
 int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st);
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
@@ -61,6 +62,8 @@ struct gastar_ctx {
     int device = 0;
     int sms = 0;
     int coop = 0;
+    size_t smem_per_sm = 0;  // shared memory of one SM
+    size_t smem_optin = 0;   // largest dynamic shared memory one block may ask for
     size_t mem_total = 0;
     char name[256] = {0};
     cudaStream_t stream = nullptr;

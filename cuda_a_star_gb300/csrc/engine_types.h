@@ -23,6 +23,25 @@ inline __host__ __device__ size_t stage_entries_per_buffer(uint32_t heaps, uint3
     return (size_t)heaps * ew * maxn;
 }
 
+// Global stage area of a multi-block team: two buffers, each one region of
+// warps*ew*maxn entries per block, followed by the per-iteration entry count
+// of every block's region (kSlots rows of `blocks` words).
+constexpr uint32_t kSlotsHost = 4;
+
+// Claim list: each warp reserves this many entries at a time; entries a warp
+// reserved but did not use hold kTouchedHole.
+constexpr uint32_t kTouchedChunk = 1024;
+constexpr uint32_t kTouchedHole = 0xffffffffu;
+
+// Warp-heap nodes below sn live in shared memory (node 0 in registers).
+constexpr uint32_t kHeapSmemNodes = 7;      // default sn: nodes 1..6
+constexpr uint32_t kHeapSmemNodesMax = 127;  // levels 0..6
+inline __host__ __device__ size_t team_stage_bytes(uint32_t blocks, uint32_t warps, uint32_t ew, uint32_t maxn,
+                                                   uint32_t entry_bytes) {
+    const size_t entries = 2 * stage_entries_per_buffer(blocks * warps, ew, maxn);
+    return ((entries * entry_bytes + (size_t)kSlotsHost * blocks * 4) + 15) & ~(size_t)15;
+}
+
 // Per-instance control block, written by the device.
 struct alignas(16) InstCtl {
     uint32_t life;        // LIFE_FRESH / LIFE_RUNNING / LIFE_DONE
@@ -77,8 +96,13 @@ struct alignas(16) TeamSlot {
 constexpr uint32_t kSlots = 4;
 
 // Control of a multi-block team (one instance on many blocks).
-struct alignas(16) TeamCtl {
-    uint32_t arrive, gen, abort, inst;  // barrier state; instance the team works on
+// The barrier counter only grows (barrier k of a team ends when it reaches
+// (k+1) x blocks) and sits on its own 128-byte line, apart from the slots
+// that every block updates with atomics.
+struct alignas(128) TeamCtl {
+    unsigned long long arrive;  // barrier arrivals since the team started
+    uint32_t abort, inst;       // a block gave up; instance the team works on
+    uint32_t pad[28];
     TeamSlot slot[kSlots];
 };
 
@@ -89,7 +113,7 @@ struct LaunchParams {
     const uint32_t* order;    // schedule order (nullptr = 0..n-1)
     uint32_t* next;           // work counter for single-block teams
     uint32_t team_ctas;       // 1 = one block per instance; >1 = all blocks on instance 0
-    uint32_t pad;
+    uint32_t heap_snodes;     // shared-memory heap nodes per warp + 1 (0 = kHeapSmemNodes)
     TeamCtl* team;            // multi-block team control (device)
     void* stage;              // multi-block stage buffer (device)
     uint64_t barrier_timeout_ns;

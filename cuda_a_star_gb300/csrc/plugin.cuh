@@ -119,6 +119,8 @@ struct PluginDom {
     static constexpr int MAXN = MAXN_;
     static constexpr bool kDense = false;
     static constexpr uint32_t kRootCode = 0xffffffffu;
+    static constexpr bool kParentBySlot = true;  // no inverse moves: parents by table slot
+    struct Look {};                              // the own-slot lookup precedes the probes
     using KeyT = PlainKey<KW>;
     using Tab = HashTabLock<KW>;
     using Pre = int;
@@ -194,11 +196,16 @@ struct PluginDom {
         slot = i;
         return r;
     }
-    static __device__ __forceinline__ int claim_first(const Tab& t, const KeyT& k, uint64_t& slot) {
-        return lock_claim<KW>(t, k, slot);
+    static __device__ __forceinline__ int claim_first(const Tab& t, const KeyT& k, uint64_t, uint64_t& slot,
+                                                      uint64_t&) {
+        const int r = lock_claim<KW>(t, k, slot);
+        return r < 0 ? r : kClNeedMin | r;
     }
-    static __device__ __forceinline__ int claim_probe(const Tab&, const KeyT&, uint64_t&) { return -1; }
-    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, uint64_t v) {
+    static __device__ __forceinline__ int claim_probe(const Tab&, const KeyT&, uint64_t, uint64_t&, uint64_t&) {
+        return -1;
+    }
+    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, const KeyT&, uint64_t v,
+                                                      uint64_t) {
         return atomicMin(t.s + slot * Tab::SW + 1 + KW, v);
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, const KeyT& k) { return k == c.goal; }
@@ -228,7 +235,7 @@ struct PluginDom {
 
 // One plugin instance on every block of the launch (cooperative when the
 // team has more than one block).
-template <class D> __global__ void __launch_bounds__(512, 1) plugin_search_kernel(LaunchParams P) {
+template <class D> __global__ void __launch_bounds__(256, 1) plugin_search_kernel(LaunchParams P) {
     __shared__ CtaShared sm;
     __shared__ typename D::Ctx ctx;
     if (threadIdx.x == 0) sm.desc = P.insts[0];

@@ -115,6 +115,25 @@ template <int N> struct SlidingDom {
     static __device__ __forceinline__ uint32_t start_f(const Ctx&, const InstDesc& d) { return d.f0; }
     // Parents are recorded by move code; the root's code is kRootMove.
     static constexpr uint32_t kRootCode = kRootMove;
+    static constexpr bool kParentBySlot = false;
+    struct Look {
+        uint64_t k, v;
+    };
+    static __device__ __forceinline__ Look look_begin(const Tab& t, KeyT k) {
+        if constexpr (KW == 1) {
+            const Look64 l = tab_look_begin(t, k);
+            return Look{l.k, l.v};
+        } else {
+            return Look{0, 0};
+        }
+    }
+    static __device__ __forceinline__ uint64_t look_end(const Tab& t, KeyT k, const Look& l) {
+        if constexpr (KW == 1) {
+            if (l.k == k) return l.v;
+            if (l.k == kEmpty) return kEmpty;
+        }
+        return get(t, k);
+    }
     static __device__ __forceinline__ uint64_t get_self(const Tab& t, KeyT k, uint32_t&) { return get(t, k); }
     static __device__ __forceinline__ uint32_t code(int m, uint32_t) { return (uint32_t)m; }
     static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
@@ -123,16 +142,20 @@ template <int N> struct SlidingDom {
         else return tab_insert(t, uint64_t(k), uint64_t(k >> 64), v, old, slot);
     }
     static constexpr bool kDense = false;
-    static __device__ __forceinline__ int claim_first(const Tab& t, KeyT k, uint64_t& slot) {
-        if constexpr (KW == 1) return tab_claim_first(t, k, slot);
+    static __device__ __forceinline__ int claim_first(const Tab& t, KeyT k, uint64_t v, uint64_t& slot,
+                                                      uint64_t& old) {
+        if constexpr (KW == 1) return tab_claim_first(t, k, v, slot, old);
         else return tab_claim_first(t, uint64_t(k), uint64_t(k >> 64), slot);
     }
-    static __device__ __forceinline__ int claim_probe(const Tab& t, KeyT k, uint64_t& slot) {
-        if constexpr (KW == 1) return tab_claim_probe(t, k, slot);
+    static __device__ __forceinline__ int claim_probe(const Tab& t, KeyT k, uint64_t v, uint64_t& slot,
+                                                      uint64_t& old) {
+        if constexpr (KW == 1) return tab_claim_probe(t, k, v, slot, old);
         else return tab_claim_probe(t, uint64_t(k), uint64_t(k >> 64), slot);
     }
-    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, uint64_t v) {
-        return tab_min_at(t, slot, v);
+    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, KeyT k, uint64_t v,
+                                                      uint64_t seen) {
+        if constexpr (KW == 1) return tab_min_at(t, slot, k, v, seen);
+        else return tab_min_at(t, slot, v);
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
     static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
@@ -217,6 +240,12 @@ struct GridDom {
     static __device__ __forceinline__ uint64_t get(const Tab& t, KeyT k) { return __ldcg(t.v + k); }
     static __device__ __forceinline__ uint32_t start_f(const Ctx&, const InstDesc& d) { return d.f0; }
     static constexpr uint32_t kRootCode = kRootMove;
+    static constexpr bool kParentBySlot = false;
+    struct Look {
+        uint64_t v;
+    };
+    static __device__ __forceinline__ Look look_begin(const Tab& t, KeyT k) { return Look{__ldcg(t.v + k)}; }
+    static __device__ __forceinline__ uint64_t look_end(const Tab&, KeyT, const Look& l) { return l.v; }
     static __device__ __forceinline__ uint64_t get_self(const Tab& t, KeyT k, uint32_t&) { return get(t, k); }
     static __device__ __forceinline__ uint32_t code(int m, uint32_t) { return (uint32_t)m; }
     static __device__ __forceinline__ int insert(const Tab& t, KeyT k, uint64_t v, uint64_t& old,
@@ -226,12 +255,17 @@ struct GridDom {
         return old == kEmpty ? 1 : 0;
     }
     static constexpr bool kDense = true;
-    static __device__ __forceinline__ int claim_first(const Tab&, KeyT k, uint64_t& slot) {
+    // The cell is the slot: one atomicMin claims and lowers it.
+    static __device__ __forceinline__ int claim_first(const Tab& t, KeyT k, uint64_t v, uint64_t& slot,
+                                                      uint64_t& old) {
         slot = k;
-        return 0;
+        old = atomicMin(t.v + k, v);
+        return old == kEmpty ? 1 : 0;
     }
-    static __device__ __forceinline__ int claim_probe(const Tab&, KeyT, uint64_t&) { return -1; }
-    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, uint64_t v) {
+    static __device__ __forceinline__ int claim_probe(const Tab&, KeyT, uint64_t, uint64_t&, uint64_t&) {
+        return -1;
+    }
+    static __device__ __forceinline__ uint64_t min_at(const Tab& t, uint64_t slot, KeyT, uint64_t v, uint64_t) {
         return atomicMin(t.v + slot, v);
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
@@ -272,6 +306,10 @@ struct GridDom {
 // ---------------------------------------------------------------------------
 struct CtaShared {
     TeamSlot slot[kSlots];  // team slots of a one-block team
+    TeamSlot agg;           // this block's share of the current iteration (multi-block teams)
+    unsigned long long agg_minprio;  // this block's heaps' min after the previous push
+    unsigned long long cnt[5];       // expansions, stale, generated, pushes, claims of this block
+    uint32_t agg_err_prev, pad2;
     InstDesc desc;
     uint32_t inst, ok, pad0, pad1;
     union {
@@ -284,36 +322,40 @@ struct CtaShared {
 
 extern __shared__ uint4 g_dyn_smem[];
 
-// Barrier over the blocks of a multi-block team: sense via a generation
-// counter, bounded wait (deadline on the device clock), abort flag so that
-// one block giving up releases the others.
+// Barrier over the blocks of a multi-block team: one atomic arrival on a
+// counter that only grows, a poll until it reaches the end of this barrier's
+// range, a bounded wait (deadline on the device clock), and an abort flag so
+// that one block giving up releases the others.
 __device__ __forceinline__ bool team_sync_grid(TeamCtl* tc, uint32_t nctas, uint64_t timeout_ns,
                                                CtaShared& sm) {
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t ok = 1;
-        volatile uint32_t* vgen = &tc->gen;
-        volatile uint32_t* vab = &tc->abort;
-        const uint32_t g = *vgen;
-        __threadfence();
-        if (atomicAdd(&tc->arrive, 1u) == nctas - 1) {
-            atomicExch(&tc->arrive, 0u);
-            __threadfence();
-            atomicAdd(&tc->gen, 1u);
-        } else {
+        // Release: the block's writes (ordered before thread 0 by the block
+        // barrier) become visible before the arrival does.
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        const unsigned long long old = atomicAdd(&tc->arrive, 1ull);
+        const unsigned long long target = (old / nctas + 1) * nctas;
+        const volatile unsigned long long* va = &tc->arrive;
+        const volatile uint32_t* vab = &tc->abort;
+        if (*va < target) {
             const uint64_t t0 = globaltimer_ns();
             for (uint32_t spin = 1;; ++spin) {
-                if (*vgen != g) break;
-                if (*vab) { ok = 0; break; }
+                if (*va >= target) break;
+                if (*vab) {
+                    ok = 0;
+                    break;
+                }
                 if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
                     atomicExch(&tc->abort, 1u);
                     ok = 0;
                     break;
                 }
-                __nanosleep(32);
+                if (spin > 64) __nanosleep(32);
             }
         }
-        __threadfence();
+        // Acquire: the other blocks' writes before their arrivals are visible.
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         if (*vab) ok = 0;
         sm.ok = ok;
     }
@@ -386,7 +428,8 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     WarpHeap<KW> hp;
     const uint32_t hid = rank * W + warp;
     hp.nodes = reinterpret_cast<E*>(d.heap_nodes) + (size_t)hid * (d.heap_cap + 1) * 32;
-    hp.snodes = snodes_all + (size_t)warp * (kHeapSmemNodes - 1) * 32;
+    hp.sn = P.heap_snodes ? P.heap_snodes : kHeapSmemNodes;
+    hp.snodes = snodes_all + (size_t)warp * (hp.sn - 1) * 32;
     hp.hdr = d.heap_hdr + 2 * hid;
     hp.cap = d.heap_cap;
 
@@ -411,7 +454,8 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         if (d.touched) {
             const uint64_t cnt = ld_vol64(d.touched_count);
             for (uint64_t i = tid; i < cnt; i += stride) {
-                const uint64_t w = __ldcg(d.touched + i);
+                const uint32_t w = __ldcg(d.touched + i);
+                if (w == kTouchedHole) continue;
                 for (uint32_t j = 0; j < d.prev_slot_words; ++j) __stcg(d.table + w + j, kEmpty);
             }
         } else {
@@ -425,7 +469,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         if (!tsync()) status = ST_BARRIER;
         if (hid == 0) {
             E s = inf_entry<KW>();
-            s.prio = make_prio(D::start_f(ctx, d), 0);
+            s.prio = make_prio(D::start_f(ctx, d), 0, kRootMove);
             D::set_key(s, ctx.start);
             if (lane == 0) hp.part = s;
             hp.pc = 1;
@@ -450,13 +494,36 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     if (status == kInf && !tsync()) status = ST_BARRIER;
 
     const uint32_t ew = d.ew;
+    // This warp's current claim-list chunk (none reserved yet).
+    unsigned long long t_base = 0;
+    uint32_t t_used = kTouchedChunk;
     uint32_t fmin = D::start_f(ctx, d);  // min f over the open list at the last check
     uint32_t it = 0;
     const uint32_t it0 = ld_vol(&ctl->iterations);
+    // Multi-block teams: each block stages into its own region of the team's
+    // stage buffers and aggregates its counters and minima in shared memory;
+    // one thread publishes them before the team barrier.
+    const size_t region_cap = stage_entries_per_buffer(W, ew, MAXN);
+    uint32_t* const team_counts =
+        multi ? reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(tm.stage) + 2 * stage_cap * sizeof(E))
+              : nullptr;
+    if (threadIdx.x == 0) {
+        sm.agg.minstage = kInfPrio;
+        sm.agg.best = kInf;
+        sm.agg.err = 0;
+        sm.agg.count = 0;
+        sm.agg_minprio = kInfPrio;
+        sm.agg_err_prev = 0;
+        for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
+    }
+    __syncthreads();
     while (status == kInf) {
         const uint32_t s = it % kSlots;
         TeamSlot* S = slots + s;
-        E* const stage = stage0 + (size_t)(it & 1) * stage_cap;
+        // Where this block's warps record the iteration: the team slot itself
+        // for one-block teams (shared memory), the block aggregate otherwise.
+        TeamSlot* Sw = multi ? &sm.agg : S;
+        E* const stage = stage0 + (size_t)(it & 1) * stage_cap + (multi ? (size_t)rank * region_cap : 0);
         if (leader) {
             // Slot it+1 was last read right after the barrier of iteration
             // it-2; every block is past that point, and none writes it before
@@ -485,23 +552,30 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
-        uint32_t pm = D::kRootCode, self = 0;
+        uint32_t pm = prio_pm(e.prio), self = 0;
         bool stale = false;
         uint32_t goal_g = kInf;
-        if (act) {
-            const uint64_t v = D::get_self(tab, k, self);
-            if ((uint32_t)(v >> 32) < g) {
-                stale = true;
-                act = false;
-            } else {
-                pm = (uint32_t)v;
-            }
-        }
         if (act && D::is_goal(ctx, k)) {
-            goal_g = g;
+            // The goal is never expanded (a_star.h:80-83); its cost counts
+            // unless a lower g for it is already known.
+            if ((uint32_t)(D::get(tab, k) >> 32) >= g) goal_g = g;
             act = false;
         }
-        const unsigned bexp = __ballot_sync(kFull, act), bstale = __ballot_sync(kFull, stale);
+        typename D::Look look{};
+        if constexpr (D::kParentBySlot) {
+            // Plugins record parents by slot: the entry's own slot is needed
+            // before its successors are inserted.
+            if (act) {
+                const uint64_t v = D::get_self(tab, k, self);
+                pm = (uint32_t)v;
+                if ((uint32_t)(v >> 32) < g) {
+                    stale = true;
+                    act = false;
+                }
+            }
+        } else {
+            if (act) look = D::look_begin(tab, k);  // resolved after the probes are in flight
+        }
 
         // ---- expand: per group of moves, all successors, then all probes,
         // then all atomicMins, so each group costs ~2 memory round trips ----
@@ -509,7 +583,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         constexpr int GS = MAXN < 4 ? MAXN : 4;
         uint32_t n_gen = 0, n_claim = 0, pushed = 0;
         uint64_t smin = kInfPrio;
-        bool tfull = false;
+        bool tfull = false, range = false;
 #pragma unroll
         for (int g0 = 0; g0 < MAXN; g0 += GS) {
             KeyT nk[GS];
@@ -519,33 +593,53 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             for (int j = 0; j < GS; ++j) {
                 ok[j] = act && D::succ(ctx, k, pre, g0 + j, pm, g, h, nk[j], ng[j], nh[j]);
                 n_gen += ok[j];
+                if (ok[j] && ng[j] > kMaxG) {
+                    range = true;
+                    ok[j] = false;
+                }
                 ok[j] = ok[j] && ng[j] + nh[j] < best_r;  // cannot beat the best goal found
             }
-            uint64_t slot[GS];
+            uint64_t slot[GS], old[GS], val[GS];
             int cl[GS];
 #pragma unroll
-            for (int j = 0; j < GS; ++j) cl[j] = ok[j] ? D::claim_first(tab, nk[j], slot[j]) : -1;
+            for (int j = 0; j < GS; ++j) {
+                val[j] = make_val(ng[j], D::code(g0 + j, self));
+                old[j] = 0;
+                cl[j] = ok[j] ? D::claim_first(tab, nk[j], val[j], slot[j], old[j]) : -1;
+            }
 #pragma unroll
             for (int j = 0; j < GS; ++j) {
-                if (cl[j] == 2) cl[j] = D::claim_probe(tab, nk[j], slot[j]);
+                if (cl[j] == 2) cl[j] = D::claim_probe(tab, nk[j], val[j], slot[j], old[j]);
                 if (ok[j] && cl[j] < 0) tfull = true;
             }
-            uint64_t old[GS];
 #pragma unroll
-            for (int j = 0; j < GS; ++j)
-                old[j] = (ok[j] && cl[j] >= 0) ? D::min_at(tab, slot[j], make_val(ng[j], D::code(g0 + j, self)))
-                                               : 0ull;
+            for (int j = 0; j < GS; ++j) {
+                if (cl[j] >= kClNeedMin) {
+                    old[j] = D::min_at(tab, slot[j], nk[j], val[j], old[j]);
+                    cl[j] -= kClNeedMin;
+                }
+            }
+            if constexpr (!D::kParentBySlot) {
+                if (g0 == 0 && act && (uint32_t)(D::look_end(tab, k, look) >> 32) < g) {
+                    // Stale: the table g went below the entry's own.  The
+                    // successors just inserted are real paths and stay in the
+                    // table but are not queued; the entry with the lower g
+                    // covers them.
+                    stale = true;
+                    act = false;
+                }
+            }
             uint32_t nacc = 0, ncl = 0;
             bool acc[GS], clm[GS];
 #pragma unroll
             for (int j = 0; j < GS; ++j) {
                 const bool in = ok[j] && cl[j] >= 0;
-                acc[j] = in && (uint32_t)(old[j] >> 32) > ng[j];
-                clm[j] = in && (D::kDense ? old[j] == kEmpty : cl[j] == 1);
+                acc[j] = in && act && (uint32_t)(old[j] >> 32) > ng[j];
+                clm[j] = in && cl[j] == 1;
                 nacc += acc[j];
                 ncl += clm[j];
                 if (acc[j]) {
-                    const uint64_t pr = make_prio(ng[j] + nh[j], ng[j]);
+                    const uint64_t pr = make_prio(ng[j] + nh[j], ng[j], (uint32_t)(g0 + j));
                     smin = pr < smin ? pr : smin;
                     if (D::is_goal(ctx, nk[j]) && ng[j] < goal_g) goal_g = ng[j];
                 }
@@ -556,13 +650,13 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             const uint32_t total = __shfl_sync(kFull, incl, 31);
             if (total) {
                 uint32_t base = 0;
-                if (lane == 31) base = atomicAdd(&S->count, total);
+                if (lane == 31) base = atomicAdd(&Sw->count, total);
                 base = __shfl_sync(kFull, base, 31) + incl - nacc;
 #pragma unroll
                 for (int j = 0; j < GS; ++j) {
                     if (acc[j]) {
                         E out = inf_entry<KW>();
-                        out.prio = make_prio(ng[j] + nh[j], ng[j]);
+                        out.prio = make_prio(ng[j] + nh[j], ng[j], (uint32_t)(g0 + j));
                         D::set_key(out, nk[j]);
                         st_stage(stage + base++, out, multi);
                     }
@@ -573,19 +667,33 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 const uint32_t ci = warp_incl_sum(ncl, lane);
                 const uint32_t ct = __shfl_sync(kFull, ci, 31);
                 if (ct) {
-                    unsigned long long cb = 0;
-                    if (lane == 31) cb = atomicAdd(d.touched_count, (unsigned long long)ct);
-                    cb = __shfl_sync(kFull, cb, 31) + ci - ncl;
+                    // Fill the warp's chunk; a group that overruns it
+                    // continues in a newly reserved one.
+                    const uint32_t room = kTouchedChunk - t_used;
+                    unsigned long long nb = 0;
+                    if (ct > room) {
+                        if (lane == 0) nb = atomicAdd(d.touched_count, (unsigned long long)kTouchedChunk);
+                        nb = __shfl_sync(kFull, nb, 0);
+                    }
+                    uint32_t pos = ci - ncl;
 #pragma unroll
                     for (int j = 0; j < GS; ++j) {
                         if (clm[j]) {
-                            if (cb < d.touched_cap) d.touched[cb] = (uint32_t)slot[j];
-                            ++cb;
+                            const unsigned long long at = pos < room ? t_base + t_used + pos : nb + (pos - room);
+                            if (at < d.touched_cap) d.touched[at] = (uint32_t)slot[j];
+                            ++pos;
                         }
+                    }
+                    if (ct > room) {
+                        t_base = nb;
+                        t_used = ct - room;
+                    } else {
+                        t_used += ct;
                     }
                 }
             }
         }
+        const unsigned bexp = __ballot_sync(kFull, act), bstale = __ballot_sync(kFull, stale);
         {
             uint32_t gsum = n_gen, csum = n_claim;
 #pragma unroll
@@ -596,16 +704,53 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 goal_g = gg < goal_g ? gg : goal_g;
             }
             smin = warp_min64(smin);
-            const bool any_full = __any_sync(kFull, tfull);
+            const bool any_full = __any_sync(kFull, tfull), any_range = __any_sync(kFull, range);
             if (lane == 0) {
-                if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
-                if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
-                if (gsum) atomicAdd(&ctl->generated, (unsigned long long)gsum);
-                if (pushed) atomicAdd(&ctl->pushes, (unsigned long long)pushed);
-                if (csum) atomicAdd(&ctl->table_used, (unsigned long long)csum);
-                if (smin != kInfPrio) atomicMin(&S->minstage, (unsigned long long)smin);
-                if (goal_g != kInf) atomicMin(&S->best, goal_g);
-                if (any_full) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+                if (multi) {
+                    if (bexp) atomicAdd(&sm.cnt[0], (unsigned long long)__popc(bexp));
+                    if (bstale) atomicAdd(&sm.cnt[1], (unsigned long long)__popc(bstale));
+                    if (gsum) atomicAdd(&sm.cnt[2], (unsigned long long)gsum);
+                    if (pushed) atomicAdd(&sm.cnt[3], (unsigned long long)pushed);
+                    if (csum) atomicAdd(&sm.cnt[4], (unsigned long long)csum);
+                } else {
+                    if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
+                    if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
+                    if (gsum) atomicAdd(&ctl->generated, (unsigned long long)gsum);
+                    if (pushed) atomicAdd(&ctl->pushes, (unsigned long long)pushed);
+                    if (csum) atomicAdd(&ctl->table_used, (unsigned long long)csum);
+                }
+                if (smin != kInfPrio) atomicMin(&Sw->minstage, (unsigned long long)smin);
+                if (goal_g != kInf) atomicMin(&Sw->best, goal_g);
+                if (any_full) atomicCAS(&Sw->err, 0u, (uint32_t)ST_TABLE_FULL);
+                if (any_range) atomicCAS(&Sw->err, 0u, (uint32_t)ST_COST_RANGE);
+            }
+        }
+        if (multi) {
+            // Publish this block's share: the current iteration's slot, the
+            // previous push's heap minimum, its region's entry count.
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (sm.agg.minstage != kInfPrio) atomicMin(&S->minstage, sm.agg.minstage);
+                if (sm.agg.best != kInf) atomicMin(&S->best, sm.agg.best);
+                if (sm.agg.err) atomicCAS(&S->err, 0u, sm.agg.err);
+                __stcg(team_counts + (size_t)s * tm.ctas + rank, sm.agg.count);
+                if (it > 0) {
+                    TeamSlot* pv = slots + (it + kSlots - 1) % kSlots;
+                    if (sm.agg_minprio != kInfPrio) atomicMin(&pv->minprio, sm.agg_minprio);
+                    if (sm.agg_err_prev) atomicCAS(&pv->err, 0u, sm.agg_err_prev);
+                }
+                if (sm.cnt[0]) atomicAdd(&ctl->expansions, sm.cnt[0]);
+                if (sm.cnt[1]) atomicAdd(&ctl->stale, sm.cnt[1]);
+                if (sm.cnt[2]) atomicAdd(&ctl->generated, sm.cnt[2]);
+                if (sm.cnt[3]) atomicAdd(&ctl->pushes, sm.cnt[3]);
+                if (sm.cnt[4]) atomicAdd(&ctl->table_used, sm.cnt[4]);
+                sm.agg.minstage = kInfPrio;
+                sm.agg.best = kInf;
+                sm.agg.err = 0;
+                sm.agg.count = 0;
+                sm.agg_minprio = kInfPrio;
+                sm.agg_err_prev = 0;
+                for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
             }
         }
         if (!tsync()) {
@@ -628,7 +773,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 open_min = mp < open_min ? mp : open_min;
             }
             // An iteration that lost entries (full table or heap) proves nothing.
-            if (err == ST_TABLE_FULL || err == ST_HEAP_FULL) status = err;
+            if (err == ST_TABLE_FULL || err == ST_HEAP_FULL || err == ST_COST_RANGE) status = err;
             else if (have_prev && best_r != kInf && best_r <= prio_f(open_min)) status = ST_OK;
             else if (err) status = err;
             else if (have_prev && open_min == kInfPrio) status = ST_NO_PATH;
@@ -636,14 +781,32 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             if (open_min != kInfPrio) fmin = prio_f(open_min);
         }
 
-        // ---- push: stage chunks dealt round-robin with a rotating offset ----
+        // ---- push ----
+        // One-block teams deal the block's stage chunks round-robin with a
+        // rotating offset; in a multi-block team block r takes the region of
+        // block (r + it) mod blocks, so work moves between blocks every
+        // iteration, and its warps deal that region's chunks.
         {
-            const uint32_t total = ld_vol(&S->count);
+            uint32_t total;
+            const E* src;
+            uint32_t first, step;
+            if (multi) {
+                const uint32_t from = (rank + it) % tm.ctas;
+                total = __ldcg(team_counts + (size_t)s * tm.ctas + from);
+                src = stage0 + (size_t)(it & 1) * stage_cap + (size_t)from * region_cap;
+                first = ((uint32_t)warp + it) % (uint32_t)W;
+                step = (uint32_t)W;
+            } else {
+                total = ld_vol(&S->count);
+                src = stage;
+                first = (hid + H - it % H) % H;
+                step = H;
+            }
             const uint32_t nch = (total + 31) / 32;
             bool hfull = false;
-            for (uint32_t c = (hid + H - it % H) % H; c < nch; c += H) {
+            for (uint32_t c = first; c < nch; c += step) {
                 const uint32_t idx = c * 32 + (uint32_t)lane;
-                E x = idx < total ? ld_stage(stage + idx, multi) : inf_entry<KW>();
+                E x = idx < total ? ld_stage(src + idx, multi) : inf_entry<KW>();
                 const uint32_t m = total - c * 32 < 32 ? total - c * 32 : 32;
                 if (!heap_push(hp, x, m, lane)) {
                     hfull = true;
@@ -652,8 +815,13 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             }
             const uint64_t mp = heap_min(hp);
             if (lane == 0) {
-                atomicMin(&S->minprio, (unsigned long long)mp);
-                if (hfull) atomicCAS(&S->err, 0u, (uint32_t)ST_HEAP_FULL);
+                if (multi) {
+                    atomicMin(&sm.agg_minprio, (unsigned long long)mp);
+                    if (hfull) atomicCAS(&sm.agg_err_prev, 0u, (uint32_t)ST_HEAP_FULL);
+                } else {
+                    atomicMin(&S->minprio, (unsigned long long)mp);
+                    if (hfull) atomicCAS(&S->err, 0u, (uint32_t)ST_HEAP_FULL);
+                }
             }
         }
         ++it;
@@ -662,6 +830,9 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     }
 
     if (lane == 0) atomicMax(&ctl->max_nodes, hp.max_n);
+    if (d.touched)  // the unused rest of the warp's chunk
+        for (uint32_t i = t_used + (uint32_t)lane; i < kTouchedChunk; i += 32)
+            if (t_base + i < d.touched_cap) d.touched[t_base + i] = kTouchedHole;
     if (status == kInf) {  // suspended: keep the search state resident
         heap_save(hp, lane);
         if (leader) {
@@ -706,8 +877,13 @@ __device__ __forceinline__ void dispatch(const LaunchParams& P, CtaShared& sm, c
 //  * plain (team_ctas > 1): every block works on instance 0 (cooperative launch);
 //  * batch/serve: blocks of the heavy teams first take heavy instances together,
 //    then every block takes instances one block each from a work counter.
+// The batch/serve kernel (all kinds) runs up to 16 warps per block; the
+// one-kind kernels of the plain engine run at most 8, which leaves them twice
+// the registers.
+constexpr int max_threads_for(uint32_t kinds) { return kinds == kKindsAll ? 512 : 256; }
+
 template <uint32_t KINDS>
-__global__ void __launch_bounds__(512, 1) search_kernel(LaunchParams P) {
+__global__ void __launch_bounds__(max_threads_for(KINDS), 1) search_kernel(LaunchParams P) {
     __shared__ CtaShared sm;
     if (P.team_ctas > 1) {
         if (threadIdx.x == 0) sm.desc = P.insts[0];

@@ -253,8 +253,7 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
     if (cf.heavy_team > 1) {
         s->heavy_teams = cf.heavy_teams ? cf.heavy_teams : std::max(1u, resident / 4 / cf.heavy_team);
         s->heavy_teams = std::min(s->heavy_teams, resident / cf.heavy_team);
-        s->heavy_stage_bytes =
-            2 * stage_entries_per_buffer(cf.warps_per_block * cf.heavy_team, cf.expansion_width, 8) * 16;
+        s->heavy_stage_bytes = team_stage_bytes(cf.heavy_team, cf.warps_per_block, cf.expansion_width, 8, 16);
         if (!s->heavy_teams || !s->team_ctl.ensure(sizeof(TeamCtl) * s->heavy_teams) ||
             !s->team_stage.ensure(s->heavy_stage_bytes * s->heavy_teams))
             s->heavy_teams = 0;

@@ -35,6 +35,7 @@ enum gastar_status {
     GASTAR_NO_DEVICE = 10,     /* no usable GPU */
     GASTAR_PENDING = 11,       /* serving: request not finished yet */
     GASTAR_OUT_OF_MEMORY = 12, /* device memory budget exceeded */
+    GASTAR_COST_RANGE = 13,    /* a path cost reached 2^24 (the engine's cost range) */
 };
 
 enum gastar_heuristic {

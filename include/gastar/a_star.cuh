@@ -78,7 +78,7 @@ std::pair<std::vector<T>, std::chrono::nanoseconds> solve(const T& start, const 
     cudaDeviceProp prop;
     check(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
     const uint32_t ew = std::min(32u, std::max(1u, o.expansion_width));
-    const uint32_t W = std::min(16u, std::max(1u, o.warps_per_block));
+    const uint32_t W = std::min(8u, std::max(1u, o.warps_per_block));
     const uint32_t threads = W * 32;
     const uint64_t Q = num_queues ? num_queues : 4096;
     uint64_t heaps = (Q + ew - 1) / ew, blocks = (heaps + W - 1) / W;
@@ -118,7 +118,7 @@ std::pair<std::vector<T>, std::chrono::nanoseconds> solve(const T& start, const 
         table.ensure(words * 8);
         heapmem.ensure(heaps * (cap + 1) * 32 * sizeof(E));
         hdr.ensure(heaps * 8);
-        stage.ensure(std::max<size_t>(16, multi ? 2 * stage_entries_per_buffer(heaps, ew, D::MAXN) * sizeof(E) : 16));
+        stage.ensure(multi ? team_stage_bytes((uint32_t)blocks, W, ew, D::MAXN, sizeof(E)) : 16);
         desc.ensure(sizeof(InstDesc));
         ctl.ensure(sizeof(InstCtl));
         team.ensure(sizeof(TeamCtl) + 64);
