@@ -411,6 +411,19 @@ def run_ours(args) -> dict:
                                           "+ 48 B per pushed successor"},
         "clocks": clk,
     }
+    # The search's memory traffic is random 16-32 byte accesses (table slots,
+    # heap nodes): its own roofline is the device's measured random-sector
+    # rate, reported beside the streaming-copy fraction above.
+    try:
+        rg = eng.random_access_peak("gather")
+        rc = eng.random_access_peak("cas")
+        out["roofline"]["random_access"] = {
+            "gather_gbs": rg["gbs"], "cas16_gbs": rc["gbs"], "unit": "GB/s",
+            "frac_of_gather": achieved / rg["gbs"] if rg["gbs"] > 0 else None,
+            "how": "random 32-byte sector loads / random 16-byte CAS over an 8 GiB buffer, "
+                   "sectors x 32 B / kernel time (gastar_measure_random_peak)"}
+    except Exception as exc:  # reported, never silently dropped
+        out["roofline"]["random_access"] = {"error": str(exc)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         used, res, dt = _oracle_run(insts)
         costs_gpu = [r.cost for r in results[:n_inst]]

@@ -162,6 +162,14 @@ class Engine:
         _check(rc, "gastar_solve_grid_device")
         return SolveResult.from_c(res, None)
 
+    def random_access_peak(self, kind: str = "gather", buffer_bytes: int = 8 << 30) -> dict:
+        """Measured random 32-byte-sector rate (GB/s): "gather" loads or "cas"
+        16-byte compare-and-swaps, the roofline of the table and heap kernels."""
+        gbs, ms = C.c_double(), C.c_double()
+        _check(lib().gastar_measure_random_peak(self._h, buffer_bytes, 0 if kind == "gather" else 1,
+                                                C.byref(gbs), C.byref(ms)), "random_access_peak")
+        return {"kind": kind, "gbs": gbs.value, "ms": ms.value}
+
     def batch(self, **kw) -> "Batch":
         return Batch(self, **kw)
 
@@ -396,6 +404,44 @@ def parse_grid(text: str):
     sx, sy, tx, ty = (C.c_uint32() for _ in range(4))
     _check(lib().gastar_parse_grid(text.encode(), w.value, h.value, _u8p(a), C.byref(sx),
                                    C.byref(sy), C.byref(tx), C.byref(ty)), "parse_grid")
+    return a, (sx.value, sy.value), (tx.value, ty.value)
+
+
+def format_grid(weights, start, goal) -> str:
+    """The reference's grid document (a_star_pathfinding.h:223-231, 83-128)."""
+    a = np.ascontiguousarray(weights, dtype=np.uint8)
+    h, w = a.shape
+    need = C.c_size_t()
+    lib().gastar_format_grid(w, h, _u8p(a), start[0], start[1], goal[0], goal[1], None, 0,
+                             C.byref(need))
+    buf = C.create_string_buffer(need.value)
+    _check(lib().gastar_format_grid(w, h, _u8p(a), start[0], start[1], goal[0], goal[1], buf,
+                                    need.value, C.byref(need)), "format_grid")
+    return buf.value.decode()
+
+
+def encode_grid_binary(weights, start, goal) -> bytes:
+    """Binary dense grid: 32-byte header ("GAGRID1\\0", w, h, sx, sy, tx, ty as
+    little-endian u32) then the w*h weights row-major."""
+    a = np.ascontiguousarray(weights, dtype=np.uint8)
+    h, w = a.shape
+    out = np.zeros(32 + a.size, dtype=np.uint8)
+    n = C.c_size_t()
+    _check(lib().gastar_encode_grid_binary(w, h, _u8p(a), start[0], start[1], goal[0], goal[1],
+                                           _u8p(out), out.size, C.byref(n)), "encode_grid_binary")
+    return out[:n.value].tobytes()
+
+
+def decode_grid_binary(data: bytes):
+    buf = np.frombuffer(data, dtype=np.uint8).copy()
+    w, h = C.c_uint32(), C.c_uint32()
+    _check(lib().gastar_decode_grid_header(_u8p(buf), buf.size, C.byref(w), C.byref(h)),
+           "decode_grid_binary")
+    a = np.zeros((h.value, w.value), dtype=np.uint8)
+    sx, sy, tx, ty = (C.c_uint32() for _ in range(4))
+    _check(lib().gastar_decode_grid_binary(_u8p(buf), buf.size, _u8p(a), a.size, C.byref(sx),
+                                           C.byref(sy), C.byref(tx), C.byref(ty)),
+           "decode_grid_binary")
     return a, (sx.value, sy.value), (tx.value, ty.value)
 
 

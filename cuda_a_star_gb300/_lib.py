@@ -27,6 +27,8 @@ EXPORTS = [
     "gastar_serve_poll", "gastar_serve_release", "gastar_serve_stats",
     "gastar_parse_sliding", "gastar_format_sliding", "gastar_parse_grid_dims",
     "gastar_parse_grid", "gastar_gen_sliding", "gastar_gen_grid",
+    "gastar_format_grid", "gastar_encode_grid_binary", "gastar_decode_grid_header",
+    "gastar_decode_grid_binary", "gastar_measure_random_peak",
 ]
 
 
@@ -37,7 +39,7 @@ class Config(C.Structure):
         ("max_blocks", C.c_uint32), ("load_factor", C.c_float), ("table_log2", C.c_uint32),
         ("heap_entries", C.c_uint64), ("max_expansions", C.c_uint64),
         ("max_iterations", C.c_uint32), ("timeout_ms", C.c_uint32), ("regrow", C.c_uint32),
-        ("delta", C.c_uint32), ("stream", C.c_void_p),
+        ("delta", C.c_uint32), ("open_list", C.c_uint32), ("stream", C.c_void_p),
     ]
 
 
@@ -142,6 +144,17 @@ def load(path: str | None = None) -> C.CDLL:
                                          u8p]),
         "gastar_gen_grid": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_double,
                                       C.c_uint32, C.c_uint32, u8p]),
+        "gastar_format_grid": (C.c_int, [C.c_uint32, C.c_uint32, u8p, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, C.c_uint32, C.c_char_p, C.c_size_t,
+                                         C.POINTER(C.c_size_t)]),
+        "gastar_encode_grid_binary": (C.c_int, [C.c_uint32, C.c_uint32, u8p, C.c_uint32,
+                                                C.c_uint32, C.c_uint32, C.c_uint32, u8p,
+                                                C.c_size_t, C.POINTER(C.c_size_t)]),
+        "gastar_decode_grid_header": (C.c_int, [u8p, C.c_size_t, u32p, u32p]),
+        "gastar_measure_random_peak": (C.c_int, [vp, C.c_uint64, C.c_uint32,
+                                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "gastar_decode_grid_binary": (C.c_int, [u8p, C.c_size_t, u8p, C.c_size_t, u32p, u32p,
+                                                u32p, u32p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

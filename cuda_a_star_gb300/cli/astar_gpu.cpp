@@ -8,7 +8,9 @@
 // reference always used 5, main.cu:72), --queues Q (default 4096 like
 // NUM_QUEUES, main.cu:18), --device D (main.cu:17 fixed device 1),
 // --heuristic admissible|reference|zero, --moves standard|reference,
-// --delta D (pop window).
+// --delta D (pop window); pathfinding only: --input-format text|binary (the
+// binary dense grid of gastar_encode_grid_binary) and --convert text|binary
+// (write the input grid in that format to the output and exit, no GPU).
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -39,7 +41,7 @@ uint32_t parse_u32(const std::string& flag, const std::string& v) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    std::string input, output, version;
+    std::string input, output, version, in_format = "text", convert;
     uint32_t size = 0, queues = 4096, delta = 0;
     int device = 0;
     gastar_config cfg;
@@ -54,6 +56,13 @@ int main(int argc, char** argv) {
         else if (f == "--queues") queues = parse_u32(f, v);
         else if (f == "--device") device = (int)parse_u32(f, v);
         else if (f == "--delta") delta = parse_u32(f, v);
+        else if (f == "--input-format") {
+            if (v != "text" && v != "binary") error("Unknown input format " + v);
+            in_format = v;
+        } else if (f == "--convert") {
+            if (v != "text" && v != "binary") error("Unknown output format " + v);
+            convert = v;
+        }
         else if (f == "--heuristic") {
             if (v == "admissible") cfg.heuristic = GASTAR_H_ADMISSIBLE;
             else if (v == "reference") cfg.heuristic = GASTAR_H_REFERENCE;
@@ -71,11 +80,53 @@ int main(int argc, char** argv) {
         std::stringstream ss;
         if (input.empty()) ss << std::cin.rdbuf();
         else {
-            std::ifstream in(input);
+            std::ifstream in(input, std::ios::binary);
             if (!in) error("Cannot open " + input);
             ss << in.rdbuf();
         }
         text = ss.str();
+    }
+    if ((in_format == "binary" || !convert.empty()) && version != "pathfinding")
+        error("--input-format binary and --convert apply to pathfinding only.");
+    // The grid, from either format.
+    uint32_t w = 0, h = 0, sx = 0, sy = 0, tx = 0, ty = 0;
+    std::vector<uint8_t> wts;
+    if (version == "pathfinding") {
+        if (in_format == "binary") {
+            const uint8_t* b = reinterpret_cast<const uint8_t*>(text.data());
+            if (gastar_decode_grid_header(b, text.size(), &w, &h) != GASTAR_OK) error(gastar_last_error());
+            wts.resize((size_t)w * h);
+            if (gastar_decode_grid_binary(b, text.size(), wts.data(), wts.size(), &sx, &sy, &tx, &ty) != GASTAR_OK)
+                error(gastar_last_error());
+        } else {
+            if (gastar_parse_grid_dims(text.c_str(), &w, &h) != GASTAR_OK) error(gastar_last_error());
+            wts.resize((size_t)w * h);
+            if (gastar_parse_grid(text.c_str(), w, h, wts.data(), &sx, &sy, &tx, &ty) != GASTAR_OK)
+                error(gastar_last_error());
+        }
+    }
+    if (!convert.empty()) {
+        size_t n = 0;
+        std::string bytes;
+        if (convert == "binary") {
+            bytes.resize(GASTAR_GRID_BINARY_HEADER + wts.size());
+            if (gastar_encode_grid_binary(w, h, wts.data(), sx, sy, tx, ty, reinterpret_cast<uint8_t*>(&bytes[0]),
+                                          bytes.size(), &n) != GASTAR_OK)
+                error("Cannot encode the grid.");
+        } else {
+            gastar_format_grid(w, h, wts.data(), sx, sy, tx, ty, nullptr, 0, &n);
+            bytes.resize(n);
+            if (gastar_format_grid(w, h, wts.data(), sx, sy, tx, ty, &bytes[0], bytes.size(), &n) != GASTAR_OK)
+                error("Cannot format the grid.");
+            bytes.resize(n - 1);  // without the NUL
+        }
+        if (output.empty()) std::cout.write(bytes.data(), (std::streamsize)bytes.size());
+        else {
+            std::ofstream o(output, std::ios::binary);
+            if (!o) error("Cannot open " + output);
+            o.write(bytes.data(), (std::streamsize)bytes.size());
+        }
+        return 0;
     }
     cfg.num_queues = queues;
     cfg.delta = delta;
@@ -104,11 +155,6 @@ int main(int argc, char** argv) {
             out << line << '\n';
         }
     } else {
-        uint32_t w, h, sx, sy, tx, ty;
-        if (gastar_parse_grid_dims(text.c_str(), &w, &h) != GASTAR_OK) error(gastar_last_error());
-        std::vector<uint8_t> wts((size_t)w * h);
-        if (gastar_parse_grid(text.c_str(), w, h, wts.data(), &sx, &sy, &tx, &ty) != GASTAR_OK)
-            error(gastar_last_error());
         std::vector<uint32_t> path((size_t)w * h);
         if (gastar_solve_grid(ctx, w, h, wts.data(), sx, sy, tx, ty, &cfg, path.data(), (uint32_t)path.size(),
                               &r) != GASTAR_OK)

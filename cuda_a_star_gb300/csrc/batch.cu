@@ -188,7 +188,14 @@ int batch_upload(gastar_batch* b) {
     const uint32_t n = (uint32_t)b->insts.size();
     const PartConfig pc = part_config(b);
     b->threads = pc.warps * 32;
-    b->smem = block_smem_bytes(kKindsAll, pc.warps, pc.ew, false);
+    // Shared memory for the kinds in the batch (one kernel serves all kinds).
+    uint32_t present = 0;
+    for (const Problem& p : b->insts) present |= kind_bit(p.kind);
+    b->smem = block_smem_bytes(present, pc.warps, pc.ew, false);
+    if (b->smem + 4096 > c->smem_optin) {  // + the kernel's static shared memory
+        set_error("batch: warps_per_block x expansion_width needs more shared memory than a block has");
+        return GASTAR_OUT_OF_MEMORY;
+    }
     const int nb = occupancy_blocks(c, kKindsAll, b->threads, b->smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
     b->blocks = b->cfg.blocks ? b->cfg.blocks : (uint32_t)(nb * c->sms);

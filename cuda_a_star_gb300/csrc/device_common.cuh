@@ -453,6 +453,202 @@ __device__ bool heap_push(WarpHeap<KW>& h, Entry<KW> x, uint32_t m, int lane) {
 }
 
 // ---------------------------------------------------------------------------
+// Bucket front of a warp's open list.
+//
+// Entries whose f lies in the window [lo, lo + 32) go to one of 32 buckets
+// (bucket = f mod 32; lane b keeps bucket b's state), each a stack of 32-entry
+// pages in shared memory.  Every other entry -- and every entry once the page
+// pool is used up -- goes to the warp-heap.  A pop takes from whichever holds
+// the lower f; the buckets are exact in f and last-in first-out within one f,
+// which favours the deepest entries among equal f as the heap's g tie-break
+// does, so the open list's minimum stays exact.  A push or pop costs a few
+// shared-memory accesses instead of a walk through the heap's levels.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoPage = 0xffffu;
+
+template <int KW> struct Buckets {
+    Entry<KW>* pages;  // P pages of 32 entries (shared memory)
+    uint16_t* link;    // the page below each page in its bucket's stack
+    uint16_t* fstack;  // free pages
+    uint32_t* upd;     // per-bucket scratch of a push (32 words)
+    uint32_t P;        // pages in the pool (0 = buckets off)
+    uint32_t nfree;    // free pages (warp-uniform)
+    uint32_t lo;       // window start (warp-uniform)
+    uint32_t head;     // lane b: top page of bucket b (kNoPage = empty)
+    uint32_t hcnt;     // lane b: entries in that page (the pages below are full)
+};
+
+template <int KW> __device__ __forceinline__ void bq_init(Buckets<KW>& q, int lane) {
+    q.nfree = q.P;
+    q.lo = 0;
+    q.head = kNoPage;
+    q.hcnt = 0;
+    for (uint32_t i = (uint32_t)lane; i < q.P; i += 32) q.fstack[i] = (uint16_t)i;
+    __syncwarp();
+}
+
+// f of the lowest non-empty bucket, or kInf.
+template <int KW> __device__ __forceinline__ uint32_t bq_min_f(const Buckets<KW>& q) {
+    const uint32_t mask = __ballot_sync(kFull, q.head != kNoPage);
+    if (!mask) return kInf;
+    const uint32_t s = q.lo & 31u;
+    const uint32_t rot = s ? (mask >> s) | (mask << (32 - s)) : mask;
+    return q.lo + (uint32_t)(__ffs(rot) - 1);
+}
+
+template <int KW> __device__ __forceinline__ uint64_t open_min(const WarpHeap<KW>& h, const Buckets<KW>& q) {
+    const uint64_t hm = heap_min(h);
+    if (!q.P) return hm;
+    const uint32_t bf = bq_min_f(q);
+    const uint64_t bp = bf == kInf ? kInfPrio : ((uint64_t)bf << 32);
+    return hm < bp ? hm : bp;
+}
+
+// Adds x (lanes < m valid; lanes >= m hold inf entries).  Returns false when
+// the heap is full (entries were lost).
+template <int KW>
+__device__ bool open_push(WarpHeap<KW>& h, Buckets<KW>& q, Entry<KW> x, uint32_t m, int lane) {
+    if (m == 0) return true;
+    const bool valid = (uint32_t)lane < m;
+    bool placed = false;
+    if (q.P) {
+        const uint32_t f = prio_f(x.prio);
+        if (!__any_sync(kFull, q.head != kNoPage)) {  // empty: the window starts at the least f
+            uint32_t mf = valid ? f : kInf;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint32_t t = __shfl_xor_sync(kFull, mf, o);
+                mf = t < mf ? t : mf;
+            }
+            q.lo = mf;
+        }
+        const bool inwin = valid && f >= q.lo && f - q.lo < 32u;
+        const uint32_t b = f & 31u;
+        const uint32_t lt = (1u << lane) - 1u;
+        const uint32_t grp = __match_any_sync(kFull, inwin ? b : 32u + (uint32_t)lane);
+        const uint32_t r = __popc(grp & lt), n = __popc(grp);
+        const uint32_t hd = __shfl_sync(kFull, q.head, (int)b), hc = __shfl_sync(kFull, q.hcnt, (int)b);
+        const bool leader = inwin && r == 0;
+        const uint32_t room = hd == kNoPage ? 0u : 32u - hc;
+        const bool need = inwin && n > room;
+        // One new page per overflowing bucket, from the free stack.
+        const uint32_t nmask = __ballot_sync(kFull, leader && need);
+        uint32_t page = kNoPage;
+        if (leader && need) {
+            const uint32_t idx = __popc(nmask & lt);
+            if (idx < q.nfree) page = q.fstack[q.nfree - 1 - idx];
+        }
+        const uint32_t want = __popc(nmask);
+        q.nfree -= want < q.nfree ? want : q.nfree;
+        page = __shfl_sync(kFull, page, __ffs(grp) - 1);
+        if (inwin) {
+            if (r < room) {
+                st_stage(q.pages + (size_t)hd * 32 + hc + r, x, false);
+                placed = true;
+            } else if (page != kNoPage) {
+                st_stage(q.pages + (size_t)page * 32 + (r - room), x, false);
+                placed = true;
+            }
+        }
+        if (leader) {
+            uint32_t nh = hd, nc = hc;
+            if (n <= room) {
+                nc = hc + n;
+            } else {
+                if (hd != kNoPage) nc = 32;
+                if (page != kNoPage) {
+                    q.link[page] = (uint16_t)hd;
+                    nh = page;
+                    nc = n - room;
+                }
+            }
+            q.upd[b] = (nh << 8) | nc;
+        }
+        const uint32_t umask = __reduce_or_sync(kFull, leader ? (1u << b) : 0u);
+        __syncwarp();
+        if ((umask >> lane) & 1u) {
+            const uint32_t u = q.upd[lane];
+            q.head = u >> 8;
+            q.hcnt = u & 0xffu;
+        }
+        __syncwarp();
+    }
+    const bool rest = valid && !placed;
+    const uint32_t rm = __ballot_sync(kFull, rest);
+    if (!rm) return true;
+    return heap_push(h, rest ? x : inf_entry<KW>(), (uint32_t)__popc(rm), lane);
+}
+
+// Pops up to E (1..32) entries with priority below `lim` (a multiple of 2^32
+// or kInfPrio); lane l < return value receives one.
+template <int KW>
+__device__ uint32_t open_pop(WarpHeap<KW>& h, Buckets<KW>& q, uint32_t E, uint64_t lim, Entry<KW>& out,
+                             int lane) {
+    if (!q.P) return heap_pop(h, E, lim, out, lane);
+    out = inf_entry<KW>();
+    uint32_t taken = 0;
+    for (int round = 0; round < 4 && taken < E; ++round) {
+        const uint32_t bf = bq_min_f(q);
+        const uint64_t hm = heap_min(h);
+        const uint64_t bp = bf == kInf ? kInfPrio : ((uint64_t)bf << 32);
+        if ((hm < bp ? hm : bp) >= lim) break;
+        const uint32_t i = (uint32_t)lane - taken;  // this lane's index among the new ones
+        if (hm < bp) {  // the heap holds lower f: take its entries below the buckets' f
+            Entry<KW> e;
+            const uint32_t c = heap_pop(h, E - taken, bp < lim ? bp : lim, e, lane);
+            const Entry<KW> sh = shfl_idx(e, (lane - (int)taken) & 31);
+            if ((uint32_t)lane >= taken && i < c) out = sh;
+            taken += c;
+            if (c == 0) break;
+        } else {
+            const int bl = (int)(bf & 31u);
+            const uint32_t hd = __shfl_sync(kFull, q.head, bl), hc = __shfl_sync(kFull, q.hcnt, bl);
+            const uint32_t k = E - taken < hc ? E - taken : hc;
+            if ((uint32_t)lane >= taken && i < k) out = ld_stage(q.pages + (size_t)hd * 32 + (hc - k + i), false);
+            if (hc == k) {  // the page is empty: back to the free stack
+                if (lane == bl) {
+                    q.fstack[q.nfree] = (uint16_t)hd;
+                    const uint32_t nx = q.link[hd];
+                    q.head = nx;
+                    q.hcnt = nx == kNoPage ? 0u : 32u;
+                }
+                q.nfree += 1;
+            } else if (lane == bl) {
+                q.hcnt = hc - k;
+            }
+            taken += k;
+            __syncwarp();
+        }
+    }
+    const uint32_t bf = bq_min_f(q);
+    if (bf != kInf) q.lo = bf;  // the window follows the lowest non-empty bucket
+    return taken;
+}
+
+// Moves every bucket entry into the heap (before the heap is saved).
+// Returns false when the heap ran full.
+template <int KW> __device__ bool open_drain(WarpHeap<KW>& h, Buckets<KW>& q, int lane) {
+    if (!q.P) return true;
+    bool ok = true;
+    for (uint32_t guard = 0; guard <= q.P; ++guard) {
+        const uint32_t mask = __ballot_sync(kFull, q.head != kNoPage);
+        if (!mask) break;
+        const int bl = __ffs(mask) - 1;
+        const uint32_t hd = __shfl_sync(kFull, q.head, bl), hc = __shfl_sync(kFull, q.hcnt, bl);
+        const Entry<KW> x = (uint32_t)lane < hc ? ld_stage(q.pages + (size_t)hd * 32 + lane, false) : inf_entry<KW>();
+        if (!heap_push(h, x, hc, lane)) ok = false;
+        if (lane == bl) {
+            const uint32_t nx = q.link[hd];
+            q.head = nx;
+            q.hcnt = nx == kNoPage ? 0u : 32u;
+        }
+        __syncwarp();
+    }
+    bq_init(q, lane);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
 // Duplicate-detection tables.  insert-or-min returns the previous value word;
 // the caller keeps a successor iff its g is strictly below the old g.  This is
 // the reference's NEW -> INSERTED / UPDATED / REJECTED classification

@@ -73,13 +73,17 @@ uint32_t entry_bytes(uint32_t kind) { return kind == KIND_SLIDING5 ? 32u : 16u; 
 uint32_t max_neighbours(uint32_t kind) { return kind == KIND_GRID ? 8u : 4u; }
 uint32_t key_words(uint32_t kind) { return kind == KIND_SLIDING5 ? 2u : 1u; }
 
-size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t heap_snodes) {
-    // Two stage buffers (one-block teams) + shared-memory heap nodes per warp.
+size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t heap_snodes,
+                        uint32_t bucket_pages) {
+    // Two stage buffers (one-block teams) + per warp: shared-memory heap
+    // nodes, bucket pages, push scratch, page links and free-page stack.
     size_t best = 0;
     for (uint32_t k = 0; k < 4; ++k)
         if (kinds & kind_bit(k)) {
             const size_t stage = multi ? 0 : 2 * stage_entries_per_buffer(warps, ew, max_neighbours(k)) * entry_bytes(k);
-            best = std::max(best, stage + (size_t)warps * (heap_snodes - 1) * 32 * entry_bytes(k));
+            const size_t per_warp = (size_t)(heap_snodes - 1 + bucket_pages) * 32 * entry_bytes(k) +
+                                    (bucket_pages ? 128 + (size_t)bucket_pages * 4 : 0);
+            best = std::max(best, stage + ((size_t)warps * per_warp + 15) / 16 * 16);
         }
     return best;
 }
@@ -226,7 +230,7 @@ void gastar_config_default(gastar_config* cfg) {
     cfg->num_queues = 4096;
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
-    cfg->expansion_width = 32;
+    cfg->expansion_width = 0;  // auto
     cfg->warps_per_block = 4;
     cfg->load_factor = 0.75f;
     cfg->regrow = 1;
@@ -328,7 +332,11 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
                          uint32_t table_log2, uint64_t heap_entries, bool want_path,
                          cudaStream_t st, InstCtl& ctl_out, AttemptStats& as) {
     const uint32_t kinds = kind_bit(pp.kind);
-    const uint32_t ew = std::min(32u, std::max(1u, cfg.expansion_width ? cfg.expansion_width : 32u));
+    // Expansion width 0 = about 1024 warp-heaps per solve: wide enough pops
+    // for large Q, enough heaps (warps) to keep the SMs busy for small Q.
+    const uint32_t ew = cfg.expansion_width
+                            ? std::min(32u, cfg.expansion_width)
+                            : (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(8, (cfg.num_queues ? cfg.num_queues : 4096) / 1024));
     const uint32_t W = std::min(8u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
     const uint32_t threads = W * 32;
     const uint64_t Q = cfg.num_queues ? cfg.num_queues : 4096;
@@ -341,23 +349,33 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     uint64_t max_blocks = (uint64_t)nb * c->sms;
     if (cfg.max_blocks) max_blocks = std::min<uint64_t>(max_blocks, cfg.max_blocks);
     if (blocks > max_blocks) blocks = max_blocks;
-    // The heaps' top levels go to the shared memory the co-resident blocks
-    // leave free: pops and pushes then touch global nodes only deep down.
-    uint32_t snodes = kHeapSmemNodes;
+    // The shared memory the co-resident blocks leave free holds the warps'
+    // bucket pages (the open list's front), or with buckets off the heaps'
+    // top levels: pops and pushes then stay out of global memory.
+    uint32_t snodes = kHeapSmemNodes, bpages = 0;
     {
         const uint64_t per_sm = (blocks + c->sms - 1) / c->sms;
-        const size_t base = block_smem_bytes(kinds, W, ew, multi, 1);
-        const size_t node = (size_t)W * 32 * entry_bytes(pp.kind);
         const size_t reserve = 4096;  // static shared memory + per-block system share
         size_t budget = c->smem_per_sm / per_sm;
         budget = budget > reserve ? std::min(budget - reserve, c->smem_optin) : 0;
-        if (budget > base + (kHeapSmemNodes - 1) * node) {
-            const uint64_t n = 1 + (budget - base) / node;
-            const uint32_t cand = (uint32_t)std::min<uint64_t>(n, kHeapSmemNodesMax);
-            const size_t s2 = block_smem_bytes(kinds, W, ew, multi, cand);
+        const size_t eb = entry_bytes(pp.kind);
+        uint32_t cs = kHeapSmemNodes, cp = 0;
+        if (cfg.open_list == 1) {
+            const size_t base = block_smem_bytes(kinds, W, ew, multi, kHeapSmemNodes, 0) + (size_t)W * 128 + 16;
+            const size_t page = (size_t)W * (32 * eb + 4);
+            if (budget > base + 8 * page) cp = (uint32_t)std::min<size_t>((budget - base) / page, 8192);
+        } else {
+            const size_t base = block_smem_bytes(kinds, W, ew, multi, 1);
+            const size_t node = (size_t)W * 32 * eb;
+            if (budget > base + (kHeapSmemNodes - 1) * node)
+                cs = (uint32_t)std::min<uint64_t>(1 + (budget - base) / node, kHeapSmemNodesMax);
+        }
+        if (cs != kHeapSmemNodes || cp) {
+            const size_t s2 = block_smem_bytes(kinds, W, ew, multi, cs, cp);
             const int nb2 = occupancy_blocks(c, kinds, threads, s2);
             if (nb2 > 0 && (uint64_t)nb2 * c->sms >= blocks) {
-                snodes = cand;
+                snodes = cs;
+                bpages = cp;
                 smem = s2;
             }
         }
@@ -458,14 +476,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     }
     c->h_desc = d;
 
-    TeamCtl tc;
-    std::memset(&tc, 0, sizeof(tc));
-    for (auto& s : tc.slot) {
-        s.minprio = ~0ull;
-        s.minstage = ~0ull;
-        s.best = kInf;
-    }
-    c->h_team = tc;
+    team_ctl_init(c->h_team);
 
     LaunchParams P;
     std::memset(&P, 0, sizeof(P));
@@ -474,6 +485,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     P.next = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(c->team.p) + sizeof(TeamCtl));
     P.team_ctas = (uint32_t)blocks;
     P.heap_snodes = snodes;
+    P.bucket_pages = bpages;
     P.team = reinterpret_cast<TeamCtl*>(c->team.p);
     P.stage = c->stage.p;
     P.barrier_timeout_ns = 2000000000ull;

@@ -28,7 +28,7 @@ uint32_t entry_bytes(uint32_t kind);
 uint32_t max_neighbours(uint32_t kind);
 uint32_t key_words(uint32_t kind);
 size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi,
-                        uint32_t heap_snodes = kHeapSmemNodes);
+                        uint32_t heap_snodes = kHeapSmemNodes, uint32_t bucket_pages = 0);
 int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st);
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,

@@ -3,8 +3,10 @@
 
 #include <cstdint>
 
-#ifndef __CUDACC__
+#if !defined(__CUDACC__) && !defined(__host__)
 #define __host__
+#endif
+#if !defined(__CUDACC__) && !defined(__device__)
 #define __device__
 #endif
 
@@ -23,9 +25,22 @@ inline __host__ __device__ size_t stage_entries_per_buffer(uint32_t heaps, uint3
     return (size_t)heaps * ew * maxn;
 }
 
-// Global stage area of a multi-block team: two buffers, each one region of
-// warps*ew*maxn entries per block, followed by the per-iteration entry count
-// of every block's region (kSlots rows of `blocks` words).
+// Multi-block teams run their iterations without a team barrier.  Block b
+// stages its successors of iteration i into region b of stage buffer
+// i % kStageRing and then raises ready[b] to i + 1; block c pushes the region
+// of block (c + i) % blocks once that block is ready.  The termination test of
+// the cut at the start of iteration i (every block's heap minimum, goals and
+// errors) is evaluated at iteration i + kCutLag, so no block runs more than
+// kCutLag iterations ahead of another, and a stage buffer is always consumed
+// before it is written again.
+constexpr uint32_t kStageRing = 4;
+constexpr uint32_t kCutLag = 2;
+constexpr uint32_t kCuts = 16;  // cut slots in the ring (> 3 * kCutLag + 2)
+static_assert(kStageRing > kCutLag, "a stage buffer must be consumed before it is reused");
+
+// Global stage area of a multi-block team: kStageRing buffers, each one
+// region of warps*ew*maxn entries per block; then the entry count of every
+// region (kStageRing rows of `blocks` words) and the blocks' ready words.
 constexpr uint32_t kSlotsHost = 4;
 
 // Claim list: each warp reserves this many entries at a time; entries a warp
@@ -38,8 +53,8 @@ constexpr uint32_t kHeapSmemNodes = 7;      // default sn: nodes 1..6
 constexpr uint32_t kHeapSmemNodesMax = 127;  // levels 0..6
 inline __host__ __device__ size_t team_stage_bytes(uint32_t blocks, uint32_t warps, uint32_t ew, uint32_t maxn,
                                                    uint32_t entry_bytes) {
-    const size_t entries = 2 * stage_entries_per_buffer(blocks * warps, ew, maxn);
-    return ((entries * entry_bytes + (size_t)kSlotsHost * blocks * 4) + 15) & ~(size_t)15;
+    const size_t entries = kStageRing * stage_entries_per_buffer(blocks * warps, ew, maxn);
+    return ((entries * entry_bytes + (size_t)(kStageRing + 1) * blocks * 4) + 15) & ~(size_t)15;
 }
 
 // Per-instance control block, written by the device.
@@ -84,7 +99,8 @@ struct alignas(16) InstDesc {
     uint64_t start_hi[2], goal_hi[2];  // key words 2..3 (generic plugin states)
 };
 
-// Per-iteration team state; iteration t uses slot t % kSlots.
+// Per-iteration state of a one-block team (shared memory); iteration t uses
+// slot t % kSlots.
 struct alignas(16) TeamSlot {
     unsigned long long minprio;   // min priority over the team's heaps after the push phase
     unsigned long long minstage;  // min priority of the entries staged in the pop/expand phase
@@ -96,15 +112,38 @@ struct alignas(16) TeamSlot {
 constexpr uint32_t kSlots = 4;
 
 // Control of a multi-block team (one instance on many blocks).
+// One cut of a multi-block team: the state at the start of an iteration.
+struct alignas(16) CutSlot {
+    unsigned long long minprio;  // min priority over the team's heaps
+    unsigned long long claims;   // table slots the blocks claimed since their last cut
+    unsigned long long exps;     // expansions since the blocks' last cut
+    uint32_t best;               // goal costs found in the iteration before
+    uint32_t lossy;              // entries were lost (table or heap full, cost range)
+    uint32_t err;                // budget or timeout
+    uint32_t count;              // blocks that published
+};
+
 // The barrier counter only grows (barrier k of a team ends when it reaches
-// (k+1) x blocks) and sits on its own 128-byte line, apart from the slots
+// (k+1) x blocks) and sits on its own 128-byte line, apart from the cut slots
 // that every block updates with atomics.
 struct alignas(128) TeamCtl {
     unsigned long long arrive;  // barrier arrivals since the team started
     uint32_t abort, inst;       // a block gave up; instance the team works on
     uint32_t pad[28];
-    TeamSlot slot[kSlots];
+    CutSlot cut[kCuts];
 };
+inline void team_ctl_init(TeamCtl& t) {
+    t.arrive = 0;
+    t.abort = 0;
+    t.inst = 0;
+    for (auto& p : t.pad) p = 0;
+    for (auto& c : t.cut) {
+        c.minprio = ~0ull;
+        c.claims = c.exps = 0;
+        c.best = 0xffffffffu;
+        c.lossy = c.err = c.count = 0;
+    }
+}
 
 struct LaunchParams {
     const InstDesc* insts;
@@ -114,6 +153,8 @@ struct LaunchParams {
     uint32_t* next;           // work counter for single-block teams
     uint32_t team_ctas;       // 1 = one block per instance; >1 = all blocks on instance 0
     uint32_t heap_snodes;     // shared-memory heap nodes per warp + 1 (0 = kHeapSmemNodes)
+    uint32_t bucket_pages;    // shared-memory bucket pages per warp (0 = heap only)
+    uint32_t pad2;
     TeamCtl* team;            // multi-block team control (device)
     void* stage;              // multi-block stage buffer (device)
     uint64_t barrier_timeout_ns;

@@ -177,6 +177,100 @@ int gastar_parse_grid(const char* text, uint32_t w, uint32_t h, uint8_t* weights
     return GASTAR_OK;
 }
 
+// The reference's grid document for a dense weight array: obstacles are the
+// cells of weight 0, costs the cells of weight other than 1 (the parser's
+// default), each list in row-major order.
+int gastar_format_grid(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx, uint32_t sy, uint32_t tx,
+                       uint32_t ty, char* out, size_t cap, size_t* written) {
+    if (!weights || !written || w == 0 || h == 0 || sx >= w || tx >= w || sy >= h || ty >= h)
+        return GASTAR_BAD_INPUT;
+    const size_t cells = (size_t)w * h;
+    size_t nobs = 0, ncost = 0;
+    for (size_t i = 0; i < cells; ++i) {
+        nobs += weights[i] == 0;
+        ncost += weights[i] > 1;
+    }
+    std::string s;
+    s.reserve(32 + nobs * 12 + ncost * 16);
+    s += std::to_string(w) + ',' + std::to_string(h) + '\n';
+    s += std::to_string(sx) + ',' + std::to_string(sy) + '\n';
+    s += std::to_string(tx) + ',' + std::to_string(ty) + '\n';
+    s += std::to_string(nobs) + '\n';
+    for (size_t i = 0; i < cells; ++i)
+        if (weights[i] == 0) s += std::to_string(i % w) + ',' + std::to_string(i / w) + '\n';
+    s += std::to_string(ncost) + '\n';
+    for (size_t i = 0; i < cells; ++i)
+        if (weights[i] > 1)
+            s += std::to_string(i % w) + ',' + std::to_string(i / w) + ',' + std::to_string(weights[i]) + '\n';
+    *written = s.size() + 1;
+    if (!out || s.size() + 1 > cap) return GASTAR_PATH_CAP;
+    std::memcpy(out, s.c_str(), s.size() + 1);
+    return GASTAR_OK;
+}
+
+namespace {
+const uint8_t kGridMagic[8] = {'G', 'A', 'G', 'R', 'I', 'D', '1', 0};
+void put_u32(uint8_t* p, uint32_t v) {
+    for (int i = 0; i < 4; ++i) p[i] = (uint8_t)(v >> (8 * i));
+}
+uint32_t get_u32(const uint8_t* p) {
+    return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24;
+}
+}  // namespace
+
+int gastar_encode_grid_binary(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx, uint32_t sy,
+                              uint32_t tx, uint32_t ty, uint8_t* out, size_t cap, size_t* written) {
+    if (!weights || !written || w == 0 || h == 0 || w > 65535 || h > 65535 || sx >= w || tx >= w || sy >= h ||
+        ty >= h)
+        return GASTAR_BAD_INPUT;
+    const size_t cells = (size_t)w * h;
+    *written = GASTAR_GRID_BINARY_HEADER + cells;
+    if (!out || *written > cap) return GASTAR_PATH_CAP;
+    std::memcpy(out, kGridMagic, 8);
+    const uint32_t f[6] = {w, h, sx, sy, tx, ty};
+    for (int i = 0; i < 6; ++i) put_u32(out + 8 + 4 * i, f[i]);
+    std::memcpy(out + GASTAR_GRID_BINARY_HEADER, weights, cells);
+    return GASTAR_OK;
+}
+
+int gastar_decode_grid_header(const uint8_t* buf, size_t len, uint32_t* w, uint32_t* h) {
+    if (!buf || !w || !h || len < GASTAR_GRID_BINARY_HEADER || std::memcmp(buf, kGridMagic, 8) != 0) {
+        gastar::set_error("binary grid: bad header");
+        return GASTAR_BAD_INPUT;
+    }
+    *w = get_u32(buf + 8);
+    *h = get_u32(buf + 12);
+    if (*w == 0 || *h == 0 || *w > 65535 || *h > 65535) {
+        gastar::set_error("binary grid: bad board size");
+        return GASTAR_BAD_INPUT;
+    }
+    return GASTAR_OK;
+}
+
+int gastar_decode_grid_binary(const uint8_t* buf, size_t len, uint8_t* weights, size_t weights_cap, uint32_t* sx,
+                              uint32_t* sy, uint32_t* tx, uint32_t* ty) {
+    uint32_t w, h;
+    const int rc = gastar_decode_grid_header(buf, len, &w, &h);
+    if (rc != GASTAR_OK) return rc;
+    if (!weights || !sx || !sy || !tx || !ty) return GASTAR_BAD_INPUT;
+    const size_t cells = (size_t)w * h;
+    if (len < GASTAR_GRID_BINARY_HEADER + cells) {
+        gastar::set_error("binary grid: truncated");
+        return GASTAR_BAD_INPUT;
+    }
+    if (weights_cap < cells) return GASTAR_PATH_CAP;
+    *sx = get_u32(buf + 16);
+    *sy = get_u32(buf + 20);
+    *tx = get_u32(buf + 24);
+    *ty = get_u32(buf + 28);
+    if (*sx >= w || *tx >= w || *sy >= h || *ty >= h) {
+        gastar::set_error("binary grid: start or target outside the board");
+        return GASTAR_BAD_INPUT;
+    }
+    std::memcpy(weights, buf + GASTAR_GRID_BINARY_HEADER, cells);
+    return GASTAR_OK;
+}
+
 // Seeded sliding-puzzle instance: goal = tiles 0..n*n-1 row-major (blank in
 // cell 0); start = a random walk of L blank moves from the goal, L uniform in
 // [walk_min, walk_max], never undoing the previous move.

@@ -309,7 +309,13 @@ struct CtaShared {
     TeamSlot agg;           // this block's share of the current iteration (multi-block teams)
     unsigned long long agg_minprio;  // this block's heaps' min after the previous push
     unsigned long long cnt[5];       // expansions, stale, generated, pushes, claims of this block
-    uint32_t agg_err_prev, pad2;
+                                     // in this launch (added to the control block at exit)
+    unsigned long long pub[2];       // claims, expansions as of the last published cut
+    unsigned long long run[2];       // claims, expansions of the cuts tested so far
+    unsigned long long base[2];      // claims, expansions before this launch
+    unsigned long long t_start;      // search start on the device clock
+    uint32_t agg_err_prev;           // heap full in the previous push
+    uint32_t dec_status, dec_best, dec_fmin, push_count;  // thread 0 -> block
     InstDesc desc;
     uint32_t inst, ok, pad0, pad1;
     union {
@@ -367,6 +373,31 @@ __device__ __forceinline__ uint32_t ld_vol(const uint32_t* p) { return *(const v
 __device__ __forceinline__ uint64_t ld_vol64(const unsigned long long* p) {
     return *(const volatile unsigned long long*)p;
 }
+__device__ __forceinline__ void st_vol(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+
+// Waits (one thread) until *p >= target: bounded by the deadline, released
+// by the team's abort flag; a timeout raises the flag.  The fence after the
+// wait orders the reads that follow after the writes the waited-for block
+// made before raising *p.
+__device__ __forceinline__ bool team_wait_u32(const uint32_t* p, uint32_t target, TeamCtl* tc,
+                                              uint64_t timeout_ns) {
+    const volatile uint32_t* vp = p;
+    if (*vp < target) {
+        const volatile uint32_t* vab = &tc->abort;
+        const uint64_t t0 = globaltimer_ns();
+        for (uint32_t spin = 1;; ++spin) {
+            if (*vp >= target) break;
+            if (*vab) return false;
+            if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+                atomicExch(&tc->abort, 1u);
+                return false;
+            }
+            if (spin > 64) __nanosleep(32);
+        }
+    }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    return true;
+}
 
 // The blocks working on one instance.
 struct TeamRef {
@@ -406,10 +437,10 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     const bool multi = tm.ctas > 1;
     const uint32_t rank = tm.rank;
     const uint32_t H = d.heaps;
-    TeamSlot* slots = multi ? tm.ctl->slot : sm.slot;
+    TeamSlot* slots = sm.slot;  // one-block teams
     const size_t stage_cap = stage_entries_per_buffer(H, d.ew, MAXN);
     char* dyn = reinterpret_cast<char*>(g_dyn_smem);
-    E* const stage0 = multi ? reinterpret_cast<E*>(tm.stage) : reinterpret_cast<E*>(dyn);
+    E* const stage0 = multi ? reinterpret_cast<E*>(tm.stage) : reinterpret_cast<E*>(dyn);  // ring (multi)
     E* const snodes_all = reinterpret_cast<E*>(dyn + (multi ? 0 : 2 * stage_cap * sizeof(E)));
     InstCtl* ctl = d.ctl;
     const bool leader = rank == 0 && threadIdx.x == 0;
@@ -432,6 +463,21 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     hp.snodes = snodes_all + (size_t)warp * (hp.sn - 1) * 32;
     hp.hdr = d.heap_hdr + 2 * hid;
     hp.cap = d.heap_cap;
+    // Shared memory after the heap nodes: every warp's bucket pages, then the
+    // push scratch words, the page links and the free-page stacks.
+    Buckets<KW> bq;
+    {
+        const uint32_t BP = P.bucket_pages;
+        E* const pages_all = snodes_all + (size_t)W * (hp.sn - 1) * 32;
+        uint32_t* const upd_all = reinterpret_cast<uint32_t*>(pages_all + (size_t)W * BP * 32);
+        uint16_t* const link_all = reinterpret_cast<uint16_t*>(upd_all + (size_t)W * 32);
+        bq.P = BP;
+        bq.pages = pages_all + (size_t)warp * BP * 32;
+        bq.upd = upd_all + (size_t)warp * 32;
+        bq.link = link_all + (size_t)warp * BP;
+        bq.fstack = link_all + (size_t)W * BP + (size_t)warp * BP;
+        bq_init(bq, lane);
+    }
 
     const uint32_t life = ld_vol(&ctl->life);
     if (!multi && threadIdx.x < kSlots) {
@@ -491,6 +537,26 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         best_r = ld_vol(&ctl->best);
         have_prev = false;
     }
+    // Multi-block teams: each block stages into its own region of the ring
+    // buffers and aggregates its counters and minima in shared memory; thread
+    // 0 publishes them (ready word, cut slot).
+    const size_t region_cap = stage_entries_per_buffer(W, d.ew, MAXN);
+    uint32_t* const ring_counts =
+        multi ? reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(tm.stage) +
+                                            (size_t)kStageRing * stage_cap * sizeof(E))
+              : nullptr;
+    uint32_t* const ready = multi ? ring_counts + (size_t)kStageRing * tm.ctas : nullptr;
+    if (multi && threadIdx.x == 0) {
+        ready[rank] = 0;
+        if (rank == 0)
+            for (uint32_t k = 0; k < kCuts; ++k) {
+                CutSlot& c = tm.ctl->cut[k];
+                c.minprio = kInfPrio;
+                c.claims = c.exps = 0;
+                c.best = kInf;
+                c.lossy = c.err = c.count = 0;
+            }
+    }
     if (status == kInf && !tsync()) status = ST_BARRIER;
 
     const uint32_t ew = d.ew;
@@ -500,13 +566,6 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     uint32_t fmin = D::start_f(ctx, d);  // min f over the open list at the last check
     uint32_t it = 0;
     const uint32_t it0 = ld_vol(&ctl->iterations);
-    // Multi-block teams: each block stages into its own region of the team's
-    // stage buffers and aggregates its counters and minima in shared memory;
-    // one thread publishes them before the team barrier.
-    const size_t region_cap = stage_entries_per_buffer(W, ew, MAXN);
-    uint32_t* const team_counts =
-        multi ? reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(tm.stage) + 2 * stage_cap * sizeof(E))
-              : nullptr;
     if (threadIdx.x == 0) {
         sm.agg.minstage = kInfPrio;
         sm.agg.best = kInf;
@@ -515,16 +574,95 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         sm.agg_minprio = kInfPrio;
         sm.agg_err_prev = 0;
         for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
+        // Budgets are tested against these (no global reads per iteration).
+        sm.base[0] = ld_vol64(&ctl->table_used);
+        sm.base[1] = ld_vol64(&ctl->expansions);
+        sm.t_start = *(const volatile uint64_t*)&ctl->t_start;
+        sm.pub[0] = sm.pub[1] = sm.run[0] = sm.run[1] = 0;
     }
     __syncthreads();
+    // The first cut of a multi-block team holds the heaps as they are now.
+    if (multi) {
+        const uint64_t mp = open_min(hp, bq);
+        if (lane == 0 && mp != kInfPrio) atomicMin(&sm.agg_minprio, (unsigned long long)mp);
+    }
     while (status == kInf) {
         const uint32_t s = it % kSlots;
         TeamSlot* S = slots + s;
         // Where this block's warps record the iteration: the team slot itself
         // for one-block teams (shared memory), the block aggregate otherwise.
         TeamSlot* Sw = multi ? &sm.agg : S;
-        E* const stage = stage0 + (size_t)(it & 1) * stage_cap + (multi ? (size_t)rank * region_cap : 0);
-        if (leader) {
+        E* const stage = multi ? stage0 + ((size_t)(it % kStageRing) * tm.ctas + rank) * region_cap
+                               : stage0 + (size_t)(it & 1) * stage_cap;
+        if (multi) {
+            // ---- publish cut `it`, test cut it - kCutLag (a_star.h:260-262) ----
+            __syncthreads();  // the previous push is complete in every warp
+            if (threadIdx.x == 0) {
+                CutSlot* cuts = tm.ctl->cut;
+                uint32_t lossy = sm.agg.err ? sm.agg.err : sm.agg_err_prev, err = 0;
+                if (leader) {
+                    if (it >= 2 * kCutLag + 2) {  // every block has read it; none writes it yet
+                        CutSlot* r = cuts + (it - 2 * kCutLag - 2) % kCuts;
+                        r->minprio = kInfPrio;
+                        r->claims = r->exps = 0;
+                        r->best = kInf;
+                        r->lossy = r->err = r->count = 0;
+                    }
+                    if (d.max_iter && it0 + it + 1 >= d.max_iter) err = ST_BUDGET;
+                    if (d.timeout_ns && globaltimer_ns() - sm.t_start > d.timeout_ns) err = ST_TIMEOUT;
+                }
+                CutSlot* c = cuts + it % kCuts;
+                if (sm.agg_minprio != kInfPrio) atomicMin(&c->minprio, sm.agg_minprio);
+                if (sm.cnt[4] != sm.pub[0]) atomicAdd(&c->claims, sm.cnt[4] - sm.pub[0]);
+                if (sm.cnt[0] != sm.pub[1]) atomicAdd(&c->exps, sm.cnt[0] - sm.pub[1]);
+                sm.pub[0] = sm.cnt[4];
+                sm.pub[1] = sm.cnt[0];
+                if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
+                if (lossy) atomicCAS(&c->lossy, 0u, lossy);
+                if (err) atomicCAS(&c->err, 0u, err);
+                asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                atomicAdd(&c->count, 1u);
+                sm.agg.best = kInf;
+                sm.agg.err = 0;
+                sm.agg.count = 0;
+                sm.agg_minprio = kInfPrio;
+                sm.agg_err_prev = 0;
+                uint32_t dec = kInf, dbest = kInf, dfmin = kInf;
+                if (it >= kCutLag) {
+                    // Waits only while a block is more than kCutLag iterations behind.
+                    const CutSlot* t = cuts + (it - kCutLag) % kCuts;
+                    if (!team_wait_u32(&t->count, tm.ctas, tm.ctl, P.barrier_timeout_ns)) {
+                        dec = ST_BARRIER;
+                    } else {
+                        const uint64_t open_min = ld_vol64(&t->minprio);
+                        dbest = ld_vol(&t->best);
+                        uint32_t tl = ld_vol(&t->lossy), te = ld_vol(&t->err);
+                        // Budgets from the team's totals, the same in every block.
+                        sm.run[0] += ld_vol64(&t->claims);
+                        sm.run[1] += ld_vol64(&t->exps);
+                        if (!tl && sm.base[0] + sm.run[0] > d.table_limit) tl = ST_TABLE_FULL;
+                        if (!te && d.max_exp && sm.base[1] + sm.run[1] >= d.max_exp) te = ST_BUDGET;
+                        const uint32_t bb = dbest < best_r ? dbest : best_r;
+                        if (tl) dec = tl;  // an iteration that lost entries proves nothing
+                        else if (bb != kInf && bb <= prio_f(open_min)) dec = ST_OK;
+                        else if (te) dec = te;
+                        else if (open_min == kInfPrio) dec = ST_NO_PATH;
+                        if (open_min != kInfPrio) dfmin = prio_f(open_min);
+                    }
+                }
+                sm.dec_status = dec;
+                sm.dec_best = dbest;
+                sm.dec_fmin = dfmin;
+            }
+            __syncthreads();
+            {
+                const uint32_t db = sm.dec_best;
+                best_r = db < best_r ? db : best_r;
+                if (sm.dec_fmin != kInf) fmin = sm.dec_fmin;
+                status = sm.dec_status;
+            }
+            if (status != kInf) break;
+        } else if (leader) {
             // Slot it+1 was last read right after the barrier of iteration
             // it-2; every block is past that point, and none writes it before
             // the barrier of this iteration.
@@ -534,10 +672,10 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             nx->count = 0;
             nx->best = kInf;
             nx->err = 0;
-            if (ld_vol64(&ctl->table_used) > d.table_limit) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
-            if (d.max_exp && ld_vol64(&ctl->expansions) >= d.max_exp) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
+            if (sm.base[0] + sm.cnt[4] > d.table_limit) atomicCAS(&S->err, 0u, (uint32_t)ST_TABLE_FULL);
+            if (d.max_exp && sm.base[1] + sm.cnt[0] >= d.max_exp) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
             if (d.max_iter && it0 + it + 1 >= d.max_iter) atomicCAS(&S->err, 0u, (uint32_t)ST_BUDGET);
-            if (d.timeout_ns && globaltimer_ns() - ctl->t_start > d.timeout_ns)
+            if (d.timeout_ns && globaltimer_ns() - sm.t_start > d.timeout_ns)
                 atomicCAS(&S->err, 0u, (uint32_t)ST_TIMEOUT);
         }
 
@@ -548,7 +686,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                                  ? ((uint64_t)(fmin + d.delta + 1) << 32)
                                  : kInfPrio;
         E e;
-        const uint32_t cnt = heap_pop(hp, ew, lim, e, lane);
+        const uint32_t cnt = open_pop(hp, bq, ew, lim, e, lane);
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;
@@ -706,19 +844,11 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             smin = warp_min64(smin);
             const bool any_full = __any_sync(kFull, tfull), any_range = __any_sync(kFull, range);
             if (lane == 0) {
-                if (multi) {
-                    if (bexp) atomicAdd(&sm.cnt[0], (unsigned long long)__popc(bexp));
-                    if (bstale) atomicAdd(&sm.cnt[1], (unsigned long long)__popc(bstale));
-                    if (gsum) atomicAdd(&sm.cnt[2], (unsigned long long)gsum);
-                    if (pushed) atomicAdd(&sm.cnt[3], (unsigned long long)pushed);
-                    if (csum) atomicAdd(&sm.cnt[4], (unsigned long long)csum);
-                } else {
-                    if (bexp) atomicAdd(&ctl->expansions, (unsigned long long)__popc(bexp));
-                    if (bstale) atomicAdd(&ctl->stale, (unsigned long long)__popc(bstale));
-                    if (gsum) atomicAdd(&ctl->generated, (unsigned long long)gsum);
-                    if (pushed) atomicAdd(&ctl->pushes, (unsigned long long)pushed);
-                    if (csum) atomicAdd(&ctl->table_used, (unsigned long long)csum);
-                }
+                if (bexp) atomicAdd(&sm.cnt[0], (unsigned long long)__popc(bexp));
+                if (bstale) atomicAdd(&sm.cnt[1], (unsigned long long)__popc(bstale));
+                if (gsum) atomicAdd(&sm.cnt[2], (unsigned long long)gsum);
+                if (pushed) atomicAdd(&sm.cnt[3], (unsigned long long)pushed);
+                if (csum) atomicAdd(&sm.cnt[4], (unsigned long long)csum);
                 if (smin != kInfPrio) atomicMin(&Sw->minstage, (unsigned long long)smin);
                 if (goal_g != kInf) atomicMin(&Sw->best, goal_g);
                 if (any_full) atomicCAS(&Sw->err, 0u, (uint32_t)ST_TABLE_FULL);
@@ -726,42 +856,35 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             }
         }
         if (multi) {
-            // Publish this block's share: the current iteration's slot, the
-            // previous push's heap minimum, its region's entry count.
-            __syncthreads();
+            // Publish this block's region, then wait for the block whose
+            // region this block pushes.
+            __syncthreads();  // every warp's stage writes are done
             if (threadIdx.x == 0) {
-                if (sm.agg.minstage != kInfPrio) atomicMin(&S->minstage, sm.agg.minstage);
-                if (sm.agg.best != kInf) atomicMin(&S->best, sm.agg.best);
-                if (sm.agg.err) atomicCAS(&S->err, 0u, sm.agg.err);
-                __stcg(team_counts + (size_t)s * tm.ctas + rank, sm.agg.count);
-                if (it > 0) {
-                    TeamSlot* pv = slots + (it + kSlots - 1) % kSlots;
-                    if (sm.agg_minprio != kInfPrio) atomicMin(&pv->minprio, sm.agg_minprio);
-                    if (sm.agg_err_prev) atomicCAS(&pv->err, 0u, sm.agg_err_prev);
-                }
-                if (sm.cnt[0]) atomicAdd(&ctl->expansions, sm.cnt[0]);
-                if (sm.cnt[1]) atomicAdd(&ctl->stale, sm.cnt[1]);
-                if (sm.cnt[2]) atomicAdd(&ctl->generated, sm.cnt[2]);
-                if (sm.cnt[3]) atomicAdd(&ctl->pushes, sm.cnt[3]);
-                if (sm.cnt[4]) atomicAdd(&ctl->table_used, sm.cnt[4]);
-                sm.agg.minstage = kInfPrio;
-                sm.agg.best = kInf;
-                sm.agg.err = 0;
+                const uint32_t row = (it % kStageRing) * tm.ctas;
+                __stcg(ring_counts + row + rank, sm.agg.count);
                 sm.agg.count = 0;
-                sm.agg_minprio = kInfPrio;
-                sm.agg_err_prev = 0;
-                for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
+                asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                st_vol(ready + rank, it + 1);
+                const uint32_t from = (rank + it) % tm.ctas;
+                uint32_t dec = kInf, n = 0;
+                if (!team_wait_u32(ready + from, it + 1, tm.ctl, P.barrier_timeout_ns)) dec = ST_BARRIER;
+                else n = __ldcg(ring_counts + row + from);
+                sm.dec_status = dec;
+                sm.push_count = n;
             }
-        }
-        if (!tsync()) {
-            status = ST_BARRIER;
-            break;
-        }
-
-        // ---- termination test (a_star.h:260-262), one iteration behind ----
-        // Open entries now: heaps after the previous push (>= that slot's
-        // min) minus this iteration's pops, plus this iteration's stage.
-        {
+            __syncthreads();
+            if (sm.dec_status != kInf) {
+                status = sm.dec_status;
+                break;
+            }
+        } else {
+            if (!tsync()) {
+                status = ST_BARRIER;
+                break;
+            }
+            // ---- termination test (a_star.h:260-262), one iteration behind ----
+            // Open entries now: heaps after the previous push (>= that slot's
+            // min) minus this iteration's pops, plus this iteration's stage.
             const uint32_t sb = ld_vol(&S->best);
             best_r = sb < best_r ? sb : best_r;
             uint32_t err = ld_vol(&S->err);
@@ -792,8 +915,8 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             uint32_t first, step;
             if (multi) {
                 const uint32_t from = (rank + it) % tm.ctas;
-                total = __ldcg(team_counts + (size_t)s * tm.ctas + from);
-                src = stage0 + (size_t)(it & 1) * stage_cap + (size_t)from * region_cap;
+                total = sm.push_count;
+                src = stage0 + ((size_t)(it % kStageRing) * tm.ctas + from) * region_cap;
                 first = ((uint32_t)warp + it) % (uint32_t)W;
                 step = (uint32_t)W;
             } else {
@@ -808,12 +931,12 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 const uint32_t idx = c * 32 + (uint32_t)lane;
                 E x = idx < total ? ld_stage(src + idx, multi) : inf_entry<KW>();
                 const uint32_t m = total - c * 32 < 32 ? total - c * 32 : 32;
-                if (!heap_push(hp, x, m, lane)) {
+                if (!open_push(hp, bq, x, m, lane)) {
                     hfull = true;
                     break;
                 }
             }
-            const uint64_t mp = heap_min(hp);
+            const uint64_t mp = open_min(hp, bq);
             if (lane == 0) {
                 if (multi) {
                     atomicMin(&sm.agg_minprio, (unsigned long long)mp);
@@ -833,6 +956,55 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     if (d.touched)  // the unused rest of the warp's chunk
         for (uint32_t i = t_used + (uint32_t)lane; i < kTouchedChunk; i += 32)
             if (t_base + i < d.touched_cap) d.touched[t_base + i] = kTouchedHole;
+    {  // this launch's counters
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (sm.cnt[0]) atomicAdd(&ctl->expansions, sm.cnt[0]);
+            if (sm.cnt[1]) atomicAdd(&ctl->stale, sm.cnt[1]);
+            if (sm.cnt[2]) atomicAdd(&ctl->generated, sm.cnt[2]);
+            if (sm.cnt[3]) atomicAdd(&ctl->pushes, sm.cnt[3]);
+            if (sm.cnt[4]) atomicAdd(&ctl->table_used, sm.cnt[4]);
+            for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
+        }
+    }
+    if (status == kInf && bq.P) {  // suspending: the buckets go back into the heap
+        if (!open_drain(hp, bq, lane) && lane == 0) atomicCAS(&sm.agg_err_prev, 0u, (uint32_t)ST_HEAP_FULL);
+        __syncthreads();
+        if (!multi && sm.agg_err_prev) status = ST_HEAP_FULL;
+    }
+    if (status == kInf) {
+        // Suspending: fold in what the iterations not tested yet found -- a
+        // goal popped there is in no heap any more -- and stop on entries
+        // they lost.
+        if (multi) {
+            if (threadIdx.x == 0) {
+                CutSlot* c = tm.ctl->cut + it % kCuts;
+                if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
+                const uint32_t lossy = sm.agg.err ? sm.agg.err : sm.agg_err_prev;
+                if (lossy) atomicCAS(&c->lossy, 0u, lossy);
+            }
+            if (!tsync()) {
+                status = ST_BARRIER;
+            } else {
+                if (threadIdx.x == 0) {
+                    uint32_t b = best_r, lossy = 0;
+                    for (uint32_t x = it > kCutLag ? it - kCutLag : 0; x <= it; ++x) {
+                        const CutSlot* c = tm.ctl->cut + x % kCuts;
+                        const uint32_t cb = ld_vol(&c->best);
+                        b = cb < b ? cb : b;
+                        if (!lossy) lossy = ld_vol(&c->lossy);
+                    }
+                    sm.dec_best = b;
+                    sm.dec_status = lossy ? lossy : kInf;
+                }
+                __syncthreads();
+                best_r = sm.dec_best;
+                status = sm.dec_status;
+            }
+        } else if (it > 0 && ld_vol(&slots[(it + kSlots - 1) % kSlots].err) == ST_HEAP_FULL) {
+            status = ST_HEAP_FULL;  // raised by the last push
+        }
+    }
     if (status == kInf) {  // suspended: keep the search state resident
         heap_save(hp, lane);
         if (leader) {
@@ -900,12 +1072,13 @@ __global__ void __launch_bounds__(max_threads_for(KINDS), 1) search_kernel(Launc
             // Every block of the team is done with the previous instance here.
             if (!team_sync_grid(tc, P.heavy_team, P.barrier_timeout_ns, sm)) break;
             if (rank == 0 && threadIdx.x == 0) {
-                for (uint32_t k = 0; k < kSlots; ++k) {
-                    tc->slot[k].minprio = kInfPrio;
-                    tc->slot[k].minstage = kInfPrio;
-                    tc->slot[k].count = 0;
-                    tc->slot[k].best = kInf;
-                    tc->slot[k].err = 0;
+                for (uint32_t k = 0; k < kCuts; ++k) {
+                    tc->cut[k].minprio = kInfPrio;
+                    tc->cut[k].claims = tc->cut[k].exps = 0;
+                    tc->cut[k].best = kInf;
+                    tc->cut[k].lossy = 0;
+                    tc->cut[k].err = 0;
+                    tc->cut[k].count = 0;
                 }
                 tc->inst = atomicAdd(P.heavy_next, 1u);
             }

@@ -241,6 +241,11 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
     cf.budget_bytes = budget;
     s->threads = cf.warps_per_block * 32;
     s->smem = block_smem_bytes(kKindsAll, cf.warps_per_block, cf.expansion_width, false);
+    if (s->smem + 4096 > c->smem_optin) {  // + the kernel's static shared memory
+        set_error("serve: warps_per_block x expansion_width needs more shared memory than a block has");
+        delete s;
+        return nullptr;
+    }
     const int nb = occupancy_blocks(c, kKindsAll, s->threads, s->smem);
     if (nb <= 0) {
         delete s;

@@ -57,7 +57,8 @@ typedef struct gastar_config {
     uint32_t num_queues;       /* parallel pops per iteration (reference Q, main.cu:18) */
     uint32_t heuristic;        /* gastar_heuristic */
     uint32_t moves;            /* gastar_moves (sliding puzzles only) */
-    uint32_t expansion_width;  /* entries each warp-heap pops per iteration, 1..32 */
+    uint32_t expansion_width;  /* entries each warp-heap pops per iteration, 1..32;
+                                  0 = auto, clamp(num_queues / 1024, 8, 32) */
     uint32_t warps_per_block;  /* warp-heaps per thread block, 1..16 */
     uint32_t max_blocks;       /* cap on thread blocks for one instance (0 = all SMs) */
     float load_factor;         /* table load limit before GASTAR_TABLE_FULL (0.5..0.9) */
@@ -68,6 +69,8 @@ typedef struct gastar_config {
     uint32_t timeout_ms;       /* device-side deadline, 0 = none */
     uint32_t regrow;           /* plain engine: re-run with doubled capacity on *_FULL (default 1) */
     uint32_t delta;            /* pop window: expand only f <= min f + delta (0 = no window) */
+    uint32_t open_list;        /* 0 = warp-heaps (top levels in shared memory);
+                                  1 = shared-memory f-buckets in front of the warp-heaps */
     void *stream;              /* cudaStream_t to launch on (NULL = the context's stream) */
 } gastar_config;
 
@@ -233,6 +236,14 @@ int gastar_serve_release(gastar_server *srv, int64_t id);
 int gastar_serve_stats(gastar_server *srv, uint32_t *waiting, uint32_t *active,
                        uint64_t *completed, uint64_t *bytes_in_use, float *kernel_ms);
 
+/* Measured random-access peak of the device, the roofline denominator of the
+ * table and heap kernels (no reference counterpart): kind 0 = random 32-byte
+ * sector loads, kind 1 = random 16-byte compare-and-swaps, over a buffer of
+ * the largest power of two <= buffer_bytes (at least 1 GiB, far above L2).
+ * *gbs = sectors x 32 bytes / kernel time; *ms = that kernel time. */
+int gastar_measure_random_peak(gastar_ctx *ctx, uint64_t buffer_bytes, uint32_t kind, double *gbs,
+                               double *ms);
+
 /* ---- text formats and synthetic instances (host only, no GPU needed) ---- */
 /* Reads "start goal" in the reference's sliding format (Position(std::istream&),
  * a_star_sliding_puzzle.h:21-48): n*n comma-separated ints, "_" or "0" = blank. */
@@ -245,6 +256,20 @@ int gastar_parse_grid_dims(const char *text, uint32_t *w, uint32_t *h);
  * dense w*h weight array: unlisted cells cost 1, obstacles 0. */
 int gastar_parse_grid(const char *text, uint32_t w, uint32_t h, uint8_t *weights, uint32_t *sx,
                       uint32_t *sy, uint32_t *tx, uint32_t *ty);
+/* The reference's grid document for a dense weight array (obstacles = weight
+ * 0, costs = weights other than 1); `*written` = bytes needed incl. the NUL. */
+int gastar_format_grid(uint32_t w, uint32_t h, const uint8_t *weights, uint32_t sx, uint32_t sy,
+                       uint32_t tx, uint32_t ty, char *out, size_t cap, size_t *written);
+/* Binary dense grid: the 8 bytes "GAGRID1\0", then w, h, sx, sy, tx, ty as
+ * little-endian u32, then the w*h weights row-major (0 = obstacle).  A 4096^2
+ * grid is 16.8 MB instead of ~200 MB of reference text.  No reference
+ * counterpart: it sits beside the text format (a_star_pathfinding.h:83-128). */
+#define GASTAR_GRID_BINARY_HEADER 32
+int gastar_encode_grid_binary(uint32_t w, uint32_t h, const uint8_t *weights, uint32_t sx, uint32_t sy,
+                              uint32_t tx, uint32_t ty, uint8_t *out, size_t cap, size_t *written);
+int gastar_decode_grid_header(const uint8_t *buf, size_t len, uint32_t *w, uint32_t *h);
+int gastar_decode_grid_binary(const uint8_t *buf, size_t len, uint8_t *weights, size_t weights_cap,
+                              uint32_t *sx, uint32_t *sy, uint32_t *tx, uint32_t *ty);
 /* Seeded instances: goal 0..n*n-1 row-major, start = non-reversing random
  * walk of uniform length in [walk_min, walk_max] (SplitMix64 stream). */
 int gastar_gen_sliding(uint32_t n, uint64_t seed, uint32_t walk_min, uint32_t walk_max,

@@ -139,12 +139,7 @@ std::pair<std::vector<T>, std::chrono::nanoseconds> solve(const T& start, const 
         d.ew = ew;
         d.ctl = static_cast<InstCtl*>(ctl.p);
         TeamCtl tc;
-        std::memset(&tc, 0, sizeof(tc));
-        for (auto& s : tc.slot) {
-            s.minprio = ~0ull;
-            s.minstage = ~0ull;
-            s.best = kInf;
-        }
+        team_ctl_init(tc);
         check(cudaMemcpy(desc.p, &d, sizeof(d), cudaMemcpyHostToDevice), "cudaMemcpy");
         check(cudaMemset(ctl.p, 0, sizeof(InstCtl)), "cudaMemset");
         check(cudaMemcpy(team.p, &tc, sizeof(tc), cudaMemcpyHostToDevice), "cudaMemcpy");

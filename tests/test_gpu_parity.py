@@ -90,6 +90,23 @@ def test_table_regrow(engine, oracle, gastar):
     _check_sliding(oracle, 4, s, g, r)
 
 
+@pytest.mark.parametrize("open_list", [0, 1])
+def test_open_list_modes(engine, oracle, gastar, open_list):
+    """Warp-heaps alone (0) and shared-memory f-buckets in front of them (1)
+    give the same optimal costs, one block and multi-block teams."""
+    for seed, queues in ((0, 32), (1, 4096), (2, 16384)):
+        s, g = gastar.gen_sliding(4, 5000 + seed, 40, 70)
+        r = engine.solve_sliding(s, g, 4, num_queues=queues, open_list=open_list)
+        _check_sliding(oracle, 4, s, g, r)
+    s, g = gastar.gen_sliding(5, 5100, 16, 24)
+    r = engine.solve_sliding(s, g, 5, num_queues=4096, open_list=open_list)
+    _check_sliding(oracle, 5, s, g, r)
+    wts = gastar.gen_grid(257, 193, 5200, 0.25)
+    for queues in (64, 8192):
+        r = engine.solve_grid(wts, (3, 2), (250, 190), num_queues=queues, open_list=open_list)
+        _check_grid(oracle, wts, (3, 2), (250, 190), r)
+
+
 def _check_grid(oracle, wts, st, gl, r):
     o, _ = oracle.grid_astar(wts, st, gl, path=False)
     if o.status == oracle.NO_PATH:
