@@ -134,7 +134,7 @@ def _mixed_instances(g):
 
 
 def run_batched(g, eng, steps: int) -> dict:
-    """configs[3]: one persistent launch over 1024 mixed instances (autotuned),
+    """Batched mixed workload: one persistent launch over 1024 instances (autotuned),
     against the plain engine on a stratified 64-instance sample of the mix."""
     import numpy as np
     p15, grids = _mixed_instances(g)
@@ -147,8 +147,8 @@ def run_batched(g, eng, steps: int) -> dict:
 
     tuner = eng.batch()
     fill(tuner)
-    cache = os.path.join(ROOT, "gpurun_out", "autotune_cache.txt") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else None
+    build_dir = os.path.join(ROOT, "cuda_a_star_gb300", "_build")
+    cache = os.path.join(build_dir, "autotune_cache.txt") if os.path.isdir(build_dir) else None
     t0 = time.perf_counter()
     tuned = tuner.autotune(sample=64, cache_path=cache)
     tune_s = time.perf_counter() - t0
@@ -230,7 +230,7 @@ def _served_requests(g):
 
 
 def run_served(g, eng) -> dict:
-    """configs[4]: the continuous-batching server under Poisson arrivals at
+    """Served mixed workload: the continuous-batching server under Poisson arrivals at
     three offered loads, calibrated to its capacity on a burst of the mix."""
     import numpy as np
     reqs = _served_requests(g)
@@ -386,11 +386,16 @@ def run_ours(args) -> dict:
     launches = sum(r.launches for r in results)
     peak, peak_kind = _peaks()
     achieved = alg_bytes / kern_s / 1e9 if kern_s > 0 else 0.0
+    # DRAM traffic per launch: ncu's traffic/algorithmic ratio of the same
+    # kernel on instances of this workload, applied to this run's launches.
     traffic = None
     prof = os.path.join(ROOT, "profiles", "search_kernel_p15.json")
-    if os.path.exists(prof):
+    searches = len(results)
+    if os.path.exists(prof) and searches:
         with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            ratio = json.load(f).get("traffic_over_algorithmic")
+        if ratio:
+            traffic = ratio * alg_bytes / searches
     out = {
         "metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -443,19 +448,41 @@ def run_ours(args) -> dict:
     return out if rank == 0 else {}
 
 
-def run_profile_case() -> None:
-    """A small copy of the workload for ncu captures (a few GB on the device):
-    4 of the 64 instances, 2^24-slot table, one pass."""
+def run_profile_case(kind: str) -> None:
+    """Small copies of the workloads for ncu captures (a few GB on the device).
+    plain: 4 of the 64 P15 instances, 2^24-slot table, one launch each.
+    batched: 32 P15 (walk 20-80) + 32 grids (side 256-512), one launch."""
     import cuda_a_star_gb300 as g
     from cuda_a_star_gb300 import build as engine_build
     engine_build.build()
+
+    def alg(r):  # algorithmic bytes of one solve
+        return 16 * (r.expansions + r.stale) + 32 * r.generated + 48 * r.pushes
+
     with g.Engine(0) as eng:
-        cfg = g.make_config(num_queues=WORKLOAD["num_queues"], table_log2=24)
-        for s, goal in _instances(g)[:4]:
-            r = eng.solve_sliding(s, goal, WORKLOAD["n"], config=cfg, path=True, path_cap=1024)
-            print(json.dumps({"status": r.status_name, "cost": r.cost, "expansions": r.expansions,
-                              "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
-                              "kernel_ms": r.kernel_ms}))
+        if kind == "plain":
+            cfg = g.make_config(num_queues=WORKLOAD["num_queues"], table_log2=24)
+            for s, goal in _instances(g)[:4]:
+                r = eng.solve_sliding(s, goal, WORKLOAD["n"], config=cfg, path=True, path_cap=1024)
+                print(json.dumps({"status": r.status_name, "cost": r.cost, "expansions": r.expansions,
+                                  "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
+                                  "iterations": r.iterations, "kernel_ms": r.kernel_ms,
+                                  "algorithmic_bytes": alg(r)}))
+            return
+        p15, grids = _mixed_instances(g)
+        b = eng.batch(warps_per_block=16, expansion_width=32, load_factor=0.5, delta_grid=18)
+        for s, goal in p15[:32]:
+            b.add_sliding(s, goal)
+        small = [(w, side) for w, side in grids if side <= 512][:32]
+        for w, side in small:
+            b.add_grid(w, (0, 0), (side - 1, side - 1))
+        b.run()
+        res = [b.result(i, path=False) for i in range(len(b))]
+        print(json.dumps({"instances": len(res), "solved": sum(r.status == g.OK for r in res),
+                          "expansions": sum(r.expansions for r in res),
+                          "algorithmic_bytes": sum(alg(r) for r in res),
+                          "stats": b.stats()}))
+        b.close()
 
 
 def main():
@@ -467,11 +494,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched mixed workload")
     ap.add_argument("--no-served", action="store_true", help="skip the served workload")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="small single pass for ncu captures (no JSON line)")
+    ap.add_argument("--profile-case", nargs="?", const="plain", choices=["plain", "batched"],
+                    help="small single pass for ncu captures (no bench JSON line)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case()
+        run_profile_case(args.profile_case)
         return
     rank, world = _dist()
     if args.impl == "reference":
