@@ -154,7 +154,7 @@ def run_batched(g, eng, steps: int) -> dict:
     tune_s = time.perf_counter() - t0
     tuner.close()
     cfgkw = {k: tuned[k] for k in ("warps_per_block", "expansion_width", "load_factor",
-                                    "delta_grid", "heavy_team")}
+                                    "delta_grid", "heavy_team", "open_list")}
     # end to end: host buffers -> upload -> solve -> results and paths back
     t0 = time.perf_counter()
     b = eng.batch(**cfgkw)
@@ -164,10 +164,11 @@ def run_batched(g, eng, steps: int) -> dict:
     e2e_s = time.perf_counter() - t0
     st0 = b.stats()
     # device-resident reruns (graph replay)
-    kms = []
+    kms, phases = [], None
     for _ in range(steps):
         b.rerun()
-        kms.append(b.stats()["kernel_ms"])
+        phases = b.stats()
+        kms.append(phases["kernel_ms"])
     res = [b.result(i, path=False) for i in range(len(b))]
     n = len(res)
     ok = sum(1 for r in res if r.status == g.OK)
@@ -195,6 +196,8 @@ def run_batched(g, eng, steps: int) -> dict:
         "instance_device_ms": {"p50": lat[n // 2], "p99": lat[min(n - 1, int(n * 0.99))],
                                "max": lat[-1]},
         "autotuned": cfgkw, "autotune_s": tune_s,
+        "last_step_phases_ms": {k: phases[k] for k in ("main_ms", "retry_ms", "promote_ms",
+                                                       "retried", "promoted")} if phases else None,
         "plain_same_mix_solves_per_s": plain_sps,
         "plain_sample": f"{len(sample)} instances (every 16th of each class), one per launch",
         "batched_over_plain": (n / (ms / 1000.0)) / plain_sps,

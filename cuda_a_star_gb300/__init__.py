@@ -233,7 +233,7 @@ class Batch:
         self.cfg = out
         return {"warps_per_block": out.warps_per_block, "expansion_width": out.expansion_width,
                 "load_factor": round(out.load_factor, 3), "delta_grid": out.delta_grid,
-                "heavy_team": out.heavy_team, "trial_ms": ms.value}
+                "heavy_team": out.heavy_team, "open_list": out.open_list, "trial_ms": ms.value}
 
     def run(self) -> None:
         _check(lib().gastar_batch_run(self._h), "gastar_batch_run")
@@ -263,8 +263,13 @@ class Batch:
     def stats(self) -> dict:
         ms, h2d, d2h, dev = C.c_float(), C.c_uint64(), C.c_uint64(), C.c_uint64()
         lib().gastar_batch_stats(self._h, C.byref(ms), C.byref(h2d), C.byref(d2h), C.byref(dev))
+        a, r, p = C.c_float(), C.c_float(), C.c_float()
+        nr, npr = C.c_uint32(), C.c_uint32()
+        lib().gastar_batch_phases(self._h, C.byref(a), C.byref(r), C.byref(p), C.byref(nr),
+                                  C.byref(npr))
         return {"kernel_ms": ms.value, "h2d_bytes": h2d.value, "d2h_bytes": d2h.value,
-                "device_bytes": dev.value}
+                "device_bytes": dev.value, "main_ms": a.value, "retry_ms": r.value,
+                "promote_ms": p.value, "retried": nr.value, "promoted": npr.value}
 
 
 class Server:

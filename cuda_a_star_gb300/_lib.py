@@ -21,7 +21,7 @@ EXPORTS = [
     "gastar_batch_config_default", "gastar_batch_create", "gastar_batch_destroy",
     "gastar_batch_add_sliding", "gastar_batch_add_grid", "gastar_batch_run",
     "gastar_batch_rerun", "gastar_batch_count", "gastar_batch_result", "gastar_batch_path",
-    "gastar_batch_stats", "gastar_batch_autotune",
+    "gastar_batch_stats", "gastar_batch_autotune", "gastar_batch_phases",
     "gastar_serve_config_default", "gastar_serve_create", "gastar_serve_destroy",
     "gastar_serve_submit_sliding", "gastar_serve_submit_grid", "gastar_serve_step",
     "gastar_serve_poll", "gastar_serve_release", "gastar_serve_stats",
@@ -60,7 +60,7 @@ class BatchConfig(C.Structure):
         ("use_graph", C.c_uint32), ("blocks", C.c_uint32), ("timeout_ms", C.c_uint32),
         ("max_expansions", C.c_uint64), ("sliding_states", C.c_uint64),
         ("delta_grid", C.c_uint32), ("heavy_team", C.c_uint32), ("heavy_cells", C.c_uint64),
-        ("promote_expansions", C.c_uint64),
+        ("promote_expansions", C.c_uint64), ("open_list", C.c_uint32), ("pad", C.c_uint32),
     ]
 
 
@@ -122,6 +122,8 @@ def load(path: str | None = None) -> C.CDLL:
         "gastar_batch_path": (C.c_int, [vp, C.c_uint32, vp, C.c_uint32, u32p]),
         "gastar_batch_stats": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "gastar_batch_phases": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float), u32p, u32p]),
         "gastar_batch_autotune": (C.c_int, [vp, C.c_uint32, C.c_char_p, C.POINTER(BatchConfig),
                                             C.POINTER(C.c_float)]),
         "gastar_serve_config_default": (None, [C.POINTER(ServeConfig)]),

@@ -66,8 +66,10 @@ struct gastar_batch {
     std::vector<uint8_t> promotable;   // re-solved by the plain engine past the budget
     uint32_t n_heavy = 0, heavy_teams = 0;
     uint64_t heavy_stage_bytes = 0;
+    uint32_t heap_snodes = kHeapSmemNodes;  // shared-memory heap nodes per warp
     DevBuf team_ctl, team_stage;
     uint32_t promoted = 0;
+    float main_ms = 0, retry_ms = 0, promote_ms = 0;  // kernel time by phase of the last run
     uint32_t retry_level = 0;   // partitions scale by 4^retry_level
     uint32_t retried = 0;       // instances re-solved with larger partitions in the last run
     bool uploaded = false;
@@ -180,24 +182,29 @@ PartConfig part_config(const gastar_batch* b) {
     pc.max_exp = cf.max_expansions;
     pc.timeout_ms = cf.timeout_ms;
     pc.retry_level = b->retry_level;
+    pc.heap_snodes = b->heap_snodes;
+    pc.buckets = cf.open_list == 1;
     return pc;
 }
 
 int batch_upload(gastar_batch* b) {
     gastar_ctx* c = b->ctx;
     const uint32_t n = (uint32_t)b->insts.size();
-    const PartConfig pc = part_config(b);
+    PartConfig pc = part_config(b);
     b->threads = pc.warps * 32;
     // Shared memory for the kinds in the batch (one kernel serves all kinds).
     uint32_t present = 0;
     for (const Problem& p : b->insts) present |= kind_bit(p.kind);
-    b->smem = block_smem_bytes(present, pc.warps, pc.ew, false);
+    b->smem = block_smem_bytes(present, pc.warps, pc.ew, false, kHeapSmemNodes, pc.buckets);
     if (b->smem + 4096 > c->smem_optin) {  // + the kernel's static shared memory
         set_error("batch: warps_per_block x expansion_width needs more shared memory than a block has");
         return GASTAR_OUT_OF_MEMORY;
     }
     const int nb = occupancy_blocks(c, kKindsAll, b->threads, b->smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
+    // The heaps' top levels take the shared memory the resident blocks leave.
+    b->heap_snodes = fit_heap_snodes(c, present, pc.warps, pc.ew, false, b->threads, nb, &b->smem, pc.buckets);
+    pc.heap_snodes = b->heap_snodes;
     b->blocks = b->cfg.blocks ? b->cfg.blocks : (uint32_t)(nb * c->sms);
     b->blocks = std::max(1u, std::min(b->blocks, n));
 
@@ -328,6 +335,8 @@ int batch_enqueue(gastar_batch* b, cudaStream_t st, bool capturing) {
     std::memset(&P, 0, sizeof(P));
     P.insts = reinterpret_cast<const InstDesc*>(b->descs.p);
     P.n_insts = b->n_sched;
+    P.heap_snodes = b->heap_snodes;
+    P.buckets = b->cfg.open_list == 1 ? 1u : 0u;
     P.order = reinterpret_cast<const uint32_t*>(b->order.p);
     P.next = reinterpret_cast<uint32_t*>(b->counters.p);
     P.team_ctas = 1;
@@ -365,6 +374,7 @@ int batch_finish(gastar_batch* b) {
     cudaStream_t st = b->ctx->stream;
     if (!cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return GASTAR_CUDA_ERROR;
     const uint32_t n = (uint32_t)b->insts.size();
+    b->retry_ms = b->promote_ms = 0;
     if (!cuda_ok(cudaEventElapsedTime(&b->kernel_ms, b->e0, b->e1), "cudaEventElapsedTime"))
         return GASTAR_CUDA_ERROR;
     b->d2h = sizeof(InstCtl) * (n + 1);
@@ -409,16 +419,21 @@ namespace {
 // fit the arena) in a follow-up batch with 4x larger partitions, then merges
 // their control blocks and paths back.  The follow-up batch retries its own
 // overflows the same way, down to 64x the class size.
+// Few overflowed instances are left to the plain engine (re-solved one at a
+// time on the whole GPU with a growing table, see batch_promote): a second
+// batch launch over a handful of instances would keep most SMs idle.
+constexpr uint32_t kPlainOverflowMax = 64;
+
+bool overflowed(uint32_t st) { return st == ST_TABLE_FULL || st == ST_HEAP_FULL || st == ST_PATH_CAP; }
+
 int batch_retry_overflows(gastar_batch* b) {
     b->retried = 0;
     if (b->retry_level >= 3) return GASTAR_OK;
     const uint32_t n = (uint32_t)b->insts.size();
     std::vector<uint32_t> bad;
-    for (uint32_t i = 0; i < n; ++i) {
-        const uint32_t st = b->h_ctl[i].status;
-        if (st == ST_TABLE_FULL || st == ST_HEAP_FULL || st == ST_PATH_CAP) bad.push_back(i);
-    }
-    if (bad.empty()) return GASTAR_OK;
+    for (uint32_t i = 0; i < n; ++i)
+        if (overflowed(b->h_ctl[i].status)) bad.push_back(i);
+    if (bad.size() <= kPlainOverflowMax) return GASTAR_OK;
     gastar_batch* sub = gastar_batch_create(b->ctx, &b->cfg);
     if (!sub) return GASTAR_OUT_OF_MEMORY;
     sub->cfg.use_graph = 0;
@@ -441,6 +456,7 @@ int batch_retry_overflows(gastar_batch* b) {
             b->h_ctl[bad[j]] = c;
         }
         b->kernel_ms += sub->kernel_ms;
+        b->retry_ms += sub->kernel_ms;
         b->h2d += sub->h2d;
         b->d2h += sub->d2h;
     }
@@ -450,13 +466,16 @@ int batch_retry_overflows(gastar_batch* b) {
 
 }  // namespace
 
-// Puzzles that used up their promotion budget in the batch are solved again
-// from scratch by the plain engine: one instance on every block of the GPU.
+// Puzzles that used up their promotion budget in the batch, and instances
+// that overflowed their partitions (when there are few of them), are solved
+// again from scratch by the plain engine: one instance on every block of the
+// GPU, its table growing as needed.
 static int batch_promote(gastar_batch* b) {
     b->promoted = 0;
     const uint32_t n = (uint32_t)b->insts.size();
     for (uint32_t i = 0; i < n; ++i) {
-        if (!b->promotable[i] || b->h_ctl[i].status != ST_BUDGET) continue;
+        const bool budget = b->promotable[i] && b->h_ctl[i].status == ST_BUDGET;
+        if (!budget && !overflowed(b->h_ctl[i].status)) continue;
         const Problem& p = b->insts[i];
         PlainProblem pp;
         std::memset(&pp, 0, sizeof(pp));
@@ -467,6 +486,12 @@ static int batch_promote(gastar_batch* b) {
         pp.goal0 = p.goal0;
         pp.goal1 = p.goal1;
         pp.f0 = p.f0;
+        if (p.kind == KIND_GRID) {  // the grid's weights are already on the device
+            pp.W = p.W;
+            pp.H = p.H;
+            pp.minw = p.minw;
+            pp.d_weights = reinterpret_cast<const uint8_t*>(b->weights.p) + b->weights_off[i];
+        }
         gastar_config cfg;
         gastar_config_default(&cfg);
         cfg.num_queues = 16384;
@@ -474,6 +499,13 @@ static int batch_promote(gastar_batch* b) {
         cfg.moves = b->cfg.moves;
         cfg.timeout_ms = b->cfg.timeout_ms;
         if (b->cfg.max_expansions) cfg.max_expansions = b->cfg.max_expansions;
+        if (p.kind == KIND_GRID) {
+            cfg.delta = b->cfg.delta_grid;
+        } else {
+            // It outgrew its partition or its budget: start large, one attempt.
+            cfg.table_log2 = p.kind == KIND_SLIDING5 ? 27 : 26;
+            cfg.heap_entries = 1ull << 25;
+        }
         std::vector<uint64_t> keys;
         gastar_result r;
         std::memset(&r, 0, sizeof(r));
@@ -497,6 +529,7 @@ static int batch_promote(gastar_batch* b) {
             b->h_paths.insert(b->h_paths.end(), keys.begin(), keys.end());
         }
         b->kernel_ms += r.kernel_ms;
+        b->promote_ms += r.kernel_ms;
         ++b->promoted;
     }
     return GASTAR_OK;
@@ -574,6 +607,17 @@ int gastar_batch_path(gastar_batch* b, uint32_t i, void* path, uint32_t cap, uin
     return GASTAR_OK;
 }
 
+int gastar_batch_phases(gastar_batch* b, float* main_ms, float* retry_ms, float* promote_ms, uint32_t* retried,
+                        uint32_t* promoted) {
+    if (!b) return GASTAR_BAD_INPUT;
+    if (main_ms) *main_ms = b->kernel_ms - b->retry_ms - b->promote_ms;
+    if (retry_ms) *retry_ms = b->retry_ms;
+    if (promote_ms) *promote_ms = b->promote_ms;
+    if (retried) *retried = b->retried;
+    if (promoted) *promoted = b->promoted;
+    return GASTAR_OK;
+}
+
 int gastar_batch_stats(gastar_batch* b, float* kernel_ms, uint64_t* h2d, uint64_t* d2h, uint64_t* dev) {
     if (!b) return GASTAR_BAD_INPUT;
     if (kernel_ms) *kernel_ms = b->kernel_ms;
@@ -624,7 +668,10 @@ bool cache_lookup(const char* path, const std::string& sig, gastar_batch_config&
         char key[600];
         unsigned w, ew, dg, team;
         float lf;
-        if (std::sscanf(line, "%599s %u %u %f %u %u", key, &w, &ew, &lf, &dg, &team) == 6 && sig == key) {
+        unsigned ol = 0;
+        const int got = std::sscanf(line, "%599s %u %u %f %u %u %u", key, &w, &ew, &lf, &dg, &team, &ol);
+        if (got >= 6 && sig == key) {
+            cfg.open_list = got == 7 ? ol : 0;
             cfg.warps_per_block = w;
             cfg.expansion_width = ew;
             cfg.load_factor = lf;
@@ -697,6 +744,9 @@ extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const cha
         }
         return GASTAR_OK;
     };
+    if ((rc = try_values([](gastar_batch_config& c, double v) { c.open_list = (uint32_t)v; }, {0, 1})) !=
+        GASTAR_OK)
+        return rc;
     if ((rc = try_values([](gastar_batch_config& c, double v) { c.warps_per_block = (uint32_t)v; },
                          {4, 8, 16})) != GASTAR_OK)
         return rc;
@@ -715,8 +765,8 @@ extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const cha
     b->cfg = best;
     if (cache_path) {
         if (FILE* f = std::fopen(cache_path, "a")) {
-            std::fprintf(f, "%s %u %u %.3f %u %u\n", sig.c_str(), best.warps_per_block, best.expansion_width,
-                         best.load_factor, best.delta_grid, best.heavy_team);
+            std::fprintf(f, "%s %u %u %.3f %u %u %u\n", sig.c_str(), best.warps_per_block, best.expansion_width,
+                         best.load_factor, best.delta_grid, best.heavy_team, best.open_list);
             std::fclose(f);
         }
     }

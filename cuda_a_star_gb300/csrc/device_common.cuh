@@ -253,6 +253,15 @@ template <int KW> __device__ __forceinline__ uint64_t node_max(const WarpHeap<KW
     return __ldcg(reinterpret_cast<const unsigned long long*>(&h.nodes[(size_t)idx * 32 + 31].prio));
 }
 
+// Starts bringing global node idx (each lane its own entry) into L2, so a
+// dependent load of it later waits for L2 instead of DRAM.
+template <int KW> __device__ __forceinline__ void prefetch_node(const WarpHeap<KW>& h, uint32_t idx, int lane) {
+    if (idx >= h.sn && idx < h.N) {
+        const Entry<KW>* a = h.nodes + (size_t)idx * 32 + lane;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    }
+}
+
 template <int KW> __device__ __forceinline__ void heap_init(WarpHeap<KW>& h) {
     h.N = 0;
     h.pc = 0;
@@ -300,6 +309,11 @@ template <int KW> __device__ void heap_sift_down(WarpHeap<KW>& h, int lane) {
         uint32_t l = 2 * idx + 1, r = l + 1;
         if (l >= h.N) break;
         Entry<KW> L = ld_node(h, l, lane);
+        // The next level is a child of l or r: start all four on their way.
+        prefetch_node(h, 2 * l + 1, lane);
+        prefetch_node(h, 2 * l + 2, lane);
+        prefetch_node(h, 2 * r + 1, lane);
+        prefetch_node(h, 2 * r + 2, lane);
         uint64_t cmax = __shfl_sync(kFull, cur.prio, 31);
         uint64_t lmin = __shfl_sync(kFull, L.prio, 0);
         if (r >= h.N) {
@@ -345,6 +359,7 @@ __device__ uint32_t heap_pop(WarpHeap<KW>& h, uint32_t E, uint64_t lim, Entry<KW
         h.pc -= c;
         return c;
     }
+    prefetch_node(h, h.N - 1, lane);  // the last node refills the root when the buffer runs short
     Entry<KW> lo, hi;
     merge2(h.root, h.part, lo, hi, lane);
     {
@@ -412,6 +427,7 @@ template <int KW> __device__ bool heap_insert_node(WarpHeap<KW>& h, Entry<KW> F,
     // that need a merge cost a dependent access.
     uint64_t pmax = kInfPrio;
     if (lane >= 1 && lane < levels) pmax = node_max(h, (p >> (levels - lane)) - 1);
+    for (int b = levels - 1; b >= 1; --b) prefetch_node(h, (p >> b) - 1, lane);  // the nodes themselves
     for (int b = levels - 1; b >= 1; --b) {
         const uint32_t idx = (p >> b) - 1;
         uint64_t fmin = __shfl_sync(kFull, F.prio, 0);
@@ -457,34 +473,42 @@ __device__ bool heap_push(WarpHeap<KW>& h, Entry<KW> x, uint32_t m, int lane) {
 //
 // Entries whose f lies in the window [lo, lo + 32) go to one of 32 buckets
 // (bucket = f mod 32; lane b keeps bucket b's state), each a stack of 32-entry
-// pages in shared memory.  Every other entry -- and every entry once the page
-// pool is used up -- goes to the warp-heap.  A pop takes from whichever holds
+// pages in global memory.  Every other entry -- and every entry once the
+// pages run out -- goes to the warp-heap.  A pop takes from whichever holds
 // the lower f; the buckets are exact in f and last-in first-out within one f,
 // which favours the deepest entries among equal f as the heap's g tie-break
-// does, so the open list's minimum stays exact.  A push or pop costs a few
-// shared-memory accesses instead of a walk through the heap's levels.
+// does, so the open list's minimum stays exact.  A push is a few shuffles and
+// stores, a pop one coalesced page load, where the heap merges 32-entry nodes
+// level by level (two 64-entry merges of ~44 shuffles each per level).
+// Pages come from a cache of free page ids held in registers (lane l < fc
+// holds one), then from never-used pages (bump), then from a stack in global
+// memory of pages freed while the cache was full.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kNoPage = 0xffffu;
+constexpr uint32_t kNoPage = 0xffffffffu;
 
 template <int KW> struct Buckets {
-    Entry<KW>* pages;  // P pages of 32 entries (shared memory)
-    uint16_t* link;    // the page below each page in its bucket's stack
-    uint16_t* fstack;  // free pages
-    uint32_t* upd;     // per-bucket scratch of a push (32 words)
-    uint32_t P;        // pages in the pool (0 = buckets off)
-    uint32_t nfree;    // free pages (warp-uniform)
+    Entry<KW>* pages;  // P pages of 32 entries (global memory)
+    uint32_t* link;    // the page below each page in its bucket's stack (global memory)
+    uint32_t* fstack;  // pages freed while the register cache was full (global memory)
+    uint32_t* upd;     // per-bucket scratch of a push (32 words, shared memory)
+    uint32_t P;        // pages (0 = buckets off)
+    uint32_t bump;     // pages >= bump were never used (warp-uniform)
+    uint32_t nfs;      // entries on fstack (warp-uniform)
+    uint32_t fc;       // free page ids cached in registers (warp-uniform)
+    uint32_t cache;    // lane l < fc: a free page id
     uint32_t lo;       // window start (warp-uniform)
     uint32_t head;     // lane b: top page of bucket b (kNoPage = empty)
     uint32_t hcnt;     // lane b: entries in that page (the pages below are full)
 };
 
-template <int KW> __device__ __forceinline__ void bq_init(Buckets<KW>& q, int lane) {
-    q.nfree = q.P;
+template <int KW> __device__ __forceinline__ void bq_init(Buckets<KW>& q, int) {
+    q.bump = 0;
+    q.nfs = 0;
+    q.fc = 0;
+    q.cache = kNoPage;
     q.lo = 0;
     q.head = kNoPage;
     q.hcnt = 0;
-    for (uint32_t i = (uint32_t)lane; i < q.P; i += 32) q.fstack[i] = (uint16_t)i;
-    __syncwarp();
 }
 
 // f of the lowest non-empty bucket, or kInf.
@@ -502,6 +526,17 @@ template <int KW> __device__ __forceinline__ uint64_t open_min(const WarpHeap<KW
     const uint32_t bf = bq_min_f(q);
     const uint64_t bp = bf == kInf ? kInfPrio : ((uint64_t)bf << 32);
     return hm < bp ? hm : bp;
+}
+
+// Returns a freed page to the cache, or to the global stack when it is full.
+template <int KW> __device__ __forceinline__ void bq_free(Buckets<KW>& q, uint32_t page, int lane) {
+    if (q.fc < 32) {
+        if ((uint32_t)lane == q.fc) q.cache = page;
+        q.fc += 1;
+    } else {
+        if (lane == 0) __stcg(q.fstack + q.nfs, page);
+        q.nfs += 1;
+    }
 }
 
 // Adds x (lanes < m valid; lanes >= m hold inf entries).  Returns false when
@@ -531,22 +566,37 @@ __device__ bool open_push(WarpHeap<KW>& h, Buckets<KW>& q, Entry<KW> x, uint32_t
         const bool leader = inwin && r == 0;
         const uint32_t room = hd == kNoPage ? 0u : 32u - hc;
         const bool need = inwin && n > room;
-        // One new page per overflowing bucket, from the free stack.
+        // One new page per overflowing bucket: cached ids first, then
+        // never-used pages, then the global stack.
         const uint32_t nmask = __ballot_sync(kFull, leader && need);
-        uint32_t page = kNoPage;
-        if (leader && need) {
-            const uint32_t idx = __popc(nmask & lt);
-            if (idx < q.nfree) page = q.fstack[q.nfree - 1 - idx];
-        }
         const uint32_t want = __popc(nmask);
-        q.nfree -= want < q.nfree ? want : q.nfree;
+        const uint32_t fresh = q.P - q.bump, avail = q.fc + fresh + q.nfs;
+        uint32_t page = kNoPage;
+        {
+            const uint32_t idx = __popc(nmask & lt);
+            const uint32_t cached = __shfl_sync(kFull, q.cache, (int)((q.fc - 1 - idx) & 31u));
+            if (leader && need && idx < avail) {
+                if (idx < q.fc) page = cached;
+                else if (idx < q.fc + fresh) page = q.bump + (idx - q.fc);
+                else page = __ldcg(q.fstack + q.nfs - 1 - (idx - q.fc - fresh));
+            }
+        }
+        {
+            uint32_t take = want < avail ? want : avail;
+            const uint32_t from_cache = take < q.fc ? take : q.fc;
+            q.fc -= from_cache;
+            take -= from_cache;
+            const uint32_t from_bump = take < fresh ? take : fresh;
+            q.bump += from_bump;
+            q.nfs -= take - from_bump;
+        }
         page = __shfl_sync(kFull, page, __ffs(grp) - 1);
         if (inwin) {
             if (r < room) {
-                st_stage(q.pages + (size_t)hd * 32 + hc + r, x, false);
+                st_entry(q.pages + (size_t)hd * 32 + hc + r, x);
                 placed = true;
             } else if (page != kNoPage) {
-                st_stage(q.pages + (size_t)page * 32 + (r - room), x, false);
+                st_entry(q.pages + (size_t)page * 32 + (r - room), x);
                 placed = true;
             }
         }
@@ -557,19 +607,19 @@ __device__ bool open_push(WarpHeap<KW>& h, Buckets<KW>& q, Entry<KW> x, uint32_t
             } else {
                 if (hd != kNoPage) nc = 32;
                 if (page != kNoPage) {
-                    q.link[page] = (uint16_t)hd;
+                    __stcg(q.link + page, hd);
                     nh = page;
                     nc = n - room;
                 }
             }
-            q.upd[b] = (nh << 8) | nc;
+            q.upd[2 * b] = nh;
+            q.upd[2 * b + 1] = nc;
         }
         const uint32_t umask = __reduce_or_sync(kFull, leader ? (1u << b) : 0u);
         __syncwarp();
         if ((umask >> lane) & 1u) {
-            const uint32_t u = q.upd[lane];
-            q.head = u >> 8;
-            q.hcnt = u & 0xffu;
+            q.head = q.upd[2 * lane];
+            q.hcnt = q.upd[2 * lane + 1];
         }
         __syncwarp();
     }
@@ -604,20 +654,19 @@ __device__ uint32_t open_pop(WarpHeap<KW>& h, Buckets<KW>& q, uint32_t E, uint64
             const int bl = (int)(bf & 31u);
             const uint32_t hd = __shfl_sync(kFull, q.head, bl), hc = __shfl_sync(kFull, q.hcnt, bl);
             const uint32_t k = E - taken < hc ? E - taken : hc;
-            if ((uint32_t)lane >= taken && i < k) out = ld_stage(q.pages + (size_t)hd * 32 + (hc - k + i), false);
-            if (hc == k) {  // the page is empty: back to the free stack
+            // The page's entries and, when it empties, its link load together.
+            const uint32_t nx = hc == k ? __ldcg(q.link + hd) : kNoPage;
+            if ((uint32_t)lane >= taken && i < k) out = ld_entry(q.pages + (size_t)hd * 32 + (hc - k + i));
+            if (hc == k) {  // the page is empty: the next one comes up, this one is free
                 if (lane == bl) {
-                    q.fstack[q.nfree] = (uint16_t)hd;
-                    const uint32_t nx = q.link[hd];
                     q.head = nx;
                     q.hcnt = nx == kNoPage ? 0u : 32u;
                 }
-                q.nfree += 1;
+                bq_free(q, hd, lane);
             } else if (lane == bl) {
                 q.hcnt = hc - k;
             }
             taken += k;
-            __syncwarp();
         }
     }
     const uint32_t bf = bq_min_f(q);
@@ -635,14 +684,13 @@ template <int KW> __device__ bool open_drain(WarpHeap<KW>& h, Buckets<KW>& q, in
         if (!mask) break;
         const int bl = __ffs(mask) - 1;
         const uint32_t hd = __shfl_sync(kFull, q.head, bl), hc = __shfl_sync(kFull, q.hcnt, bl);
-        const Entry<KW> x = (uint32_t)lane < hc ? ld_stage(q.pages + (size_t)hd * 32 + lane, false) : inf_entry<KW>();
+        const uint32_t nx = __ldcg(q.link + hd);
+        const Entry<KW> x = (uint32_t)lane < hc ? ld_entry(q.pages + (size_t)hd * 32 + lane) : inf_entry<KW>();
         if (!heap_push(h, x, hc, lane)) ok = false;
         if (lane == bl) {
-            const uint32_t nx = q.link[hd];
             q.head = nx;
             q.hcnt = nx == kNoPage ? 0u : 32u;
         }
-        __syncwarp();
     }
     bq_init(q, lane);
     return ok;

@@ -57,9 +57,12 @@ bool DevBuf::ensure(size_t bytes) {
     return true;
 }
 
-template <uint32_t K> const void* kernel_ptr() { return reinterpret_cast<const void*>(&search_kernel<K>); }
+template <uint32_t K, int T = 256> const void* kernel_ptr() {
+    return reinterpret_cast<const void*>(&search_kernel<K, T>);
+}
 
-const void* search_kernel_for(uint32_t kinds) {
+const void* search_kernel_for(uint32_t kinds, uint32_t threads) {
+    if (threads > 256) return kernel_ptr<kKindsAll, 512>();  // 9..16 warps: all kinds
     switch (kinds) {
         case kind_bit(KIND_SLIDING3): return kernel_ptr<kind_bit(KIND_SLIDING3)>();
         case kind_bit(KIND_SLIDING4): return kernel_ptr<kind_bit(KIND_SLIDING4)>();
@@ -74,22 +77,38 @@ uint32_t max_neighbours(uint32_t kind) { return kind == KIND_GRID ? 8u : 4u; }
 uint32_t key_words(uint32_t kind) { return kind == KIND_SLIDING5 ? 2u : 1u; }
 
 size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t heap_snodes,
-                        uint32_t bucket_pages) {
+                        bool buckets) {
     // Two stage buffers (one-block teams) + per warp: shared-memory heap
-    // nodes, bucket pages, push scratch, page links and free-page stack.
+    // nodes and the bucket push scratch.
     size_t best = 0;
     for (uint32_t k = 0; k < 4; ++k)
         if (kinds & kind_bit(k)) {
             const size_t stage = multi ? 0 : 2 * stage_entries_per_buffer(warps, ew, max_neighbours(k)) * entry_bytes(k);
-            const size_t per_warp = (size_t)(heap_snodes - 1 + bucket_pages) * 32 * entry_bytes(k) +
-                                    (bucket_pages ? 128 + (size_t)bucket_pages * 4 : 0);
+            const size_t per_warp = (size_t)(heap_snodes - 1) * 32 * entry_bytes(k) + (buckets ? 256 : 0);
             best = std::max(best, stage + ((size_t)warps * per_warp + 15) / 16 * 16);
         }
     return best;
 }
 
+uint32_t fit_heap_snodes(gastar_ctx* c, uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t threads,
+                         int blocks_per_sm, size_t* smem, bool buckets) {
+    *smem = block_smem_bytes(kinds, warps, ew, multi, kHeapSmemNodes, buckets);
+    if (blocks_per_sm <= 0) return kHeapSmemNodes;
+    const size_t reserve = 4096;  // static shared memory + per-block system share
+    size_t budget = c->smem_per_sm / (size_t)blocks_per_sm;
+    budget = budget > reserve ? std::min(budget - reserve, c->smem_optin - reserve) : 0;
+    const size_t base = block_smem_bytes(kinds, warps, ew, multi, 1, buckets);
+    const size_t node = block_smem_bytes(kinds, warps, ew, multi, 2, buckets) - base;  // one node in every warp
+    if (!node || budget <= base + (kHeapSmemNodes - 1) * node) return kHeapSmemNodes;
+    const uint32_t cand = (uint32_t)std::min<uint64_t>(1 + (budget - base) / node, kHeapSmemNodesMax);
+    const size_t s2 = block_smem_bytes(kinds, warps, ew, multi, cand, buckets);
+    if (occupancy_blocks(c, kinds, threads, s2) < blocks_per_sm) return kHeapSmemNodes;
+    *smem = s2;
+    return cand;
+}
+
 int occupancy_blocks(gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem) {
-    const void* f = search_kernel_for(kinds);
+    const void* f = search_kernel_for(kinds, threads);
     if (smem > 48 * 1024)
         if (!cuda_ok(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                      "cudaFuncSetAttribute"))
@@ -103,7 +122,7 @@ int occupancy_blocks(gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t sme
 
 int launch_search(gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st) {
-    const void* f = search_kernel_for(kinds);
+    const void* f = search_kernel_for(kinds, threads);
     if (smem > 48 * 1024)
         GA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     LaunchParams p = P;
@@ -278,6 +297,7 @@ void gastar_destroy(gastar_ctx* c) {
     c->table.release();
     c->dense.release();
     c->touched.release();
+    c->buckets.release();
     c->heaps.release();
     c->hdr.release();
     c->stage.release();
@@ -349,37 +369,11 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     uint64_t max_blocks = (uint64_t)nb * c->sms;
     if (cfg.max_blocks) max_blocks = std::min<uint64_t>(max_blocks, cfg.max_blocks);
     if (blocks > max_blocks) blocks = max_blocks;
-    // The shared memory the co-resident blocks leave free holds the warps'
-    // bucket pages (the open list's front), or with buckets off the heaps'
-    // top levels: pops and pushes then stay out of global memory.
-    uint32_t snodes = kHeapSmemNodes, bpages = 0;
-    {
-        const uint64_t per_sm = (blocks + c->sms - 1) / c->sms;
-        const size_t reserve = 4096;  // static shared memory + per-block system share
-        size_t budget = c->smem_per_sm / per_sm;
-        budget = budget > reserve ? std::min(budget - reserve, c->smem_optin) : 0;
-        const size_t eb = entry_bytes(pp.kind);
-        uint32_t cs = kHeapSmemNodes, cp = 0;
-        if (cfg.open_list == 1) {
-            const size_t base = block_smem_bytes(kinds, W, ew, multi, kHeapSmemNodes, 0) + (size_t)W * 128 + 16;
-            const size_t page = (size_t)W * (32 * eb + 4);
-            if (budget > base + 8 * page) cp = (uint32_t)std::min<size_t>((budget - base) / page, 8192);
-        } else {
-            const size_t base = block_smem_bytes(kinds, W, ew, multi, 1);
-            const size_t node = (size_t)W * 32 * eb;
-            if (budget > base + (kHeapSmemNodes - 1) * node)
-                cs = (uint32_t)std::min<uint64_t>(1 + (budget - base) / node, kHeapSmemNodesMax);
-        }
-        if (cs != kHeapSmemNodes || cp) {
-            const size_t s2 = block_smem_bytes(kinds, W, ew, multi, cs, cp);
-            const int nb2 = occupancy_blocks(c, kinds, threads, s2);
-            if (nb2 > 0 && (uint64_t)nb2 * c->sms >= blocks) {
-                snodes = cs;
-                bpages = cp;
-                smem = s2;
-            }
-        }
-    }
+    // The shared memory the co-resident blocks leave free holds the heaps' top
+    // levels: pops and pushes then touch global nodes only deep down.
+    const bool buckets = cfg.open_list == 1;
+    const uint32_t snodes = fit_heap_snodes(c, kinds, W, ew, multi, threads,
+                                            (int)((blocks + c->sms - 1) / c->sms), &smem, buckets);
     if (multi && !c->coop) {
         set_error("device does not support cooperative launch");
         return GASTAR_CUDA_ERROR;
@@ -437,6 +431,9 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         !c->desc.ensure(sizeof(InstDesc)) || !c->ctl.ensure(sizeof(InstCtl)) ||
         !c->team.ensure(sizeof(TeamCtl) + 64))
         return GASTAR_OUT_OF_MEMORY;
+    // Bucket front: as many pages per warp as the heap has nodes.
+    if (buckets && !c->buckets.ensure(bucket_area_bytes((uint32_t)heaps, (uint32_t)cap_nodes, ebytes)))
+        return GASTAR_OUT_OF_MEMORY;
 
     InstDesc d;
     std::memset(&d, 0, sizeof(d));
@@ -468,6 +465,10 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     d.max_iter = cfg.max_iterations;
     d.delta = cfg.delta;
     d.ctl = reinterpret_cast<InstCtl*>(c->ctl.p);
+    if (buckets) {
+        d.bq_base = c->buckets.p;
+        d.bq_pages = (uint32_t)cap_nodes;
+    }
     if (pp.kind != KIND_GRID) {
         d.touched = reinterpret_cast<uint32_t*>(c->touched.p);
         d.touched_count = reinterpret_cast<unsigned long long*>(c->misc.p);
@@ -485,7 +486,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     P.next = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(c->team.p) + sizeof(TeamCtl));
     P.team_ctas = (uint32_t)blocks;
     P.heap_snodes = snodes;
-    P.bucket_pages = bpages;
+    P.buckets = buckets ? 1u : 0u;
     P.team = reinterpret_cast<TeamCtl*>(c->team.p);
     P.stage = c->stage.p;
     P.barrier_timeout_ns = 2000000000ull;

@@ -23,16 +23,21 @@ struct DevBuf {
 void set_error(const std::string& s);
 bool cuda_ok(cudaError_t e, const char* what);
 
-const void* search_kernel_for(uint32_t kinds);
+const void* search_kernel_for(uint32_t kinds, uint32_t threads);
 uint32_t entry_bytes(uint32_t kind);
 uint32_t max_neighbours(uint32_t kind);
 uint32_t key_words(uint32_t kind);
 size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi,
-                        uint32_t heap_snodes = kHeapSmemNodes, uint32_t bucket_pages = 0);
+                        uint32_t heap_snodes = kHeapSmemNodes, bool buckets = false);
 int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st);
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
                  unsigned long long arena_words, unsigned long long* used, cudaStream_t st);
+// Largest count of shared-memory heap nodes per warp (>= kHeapSmemNodes) that
+// keeps `blocks_per_sm` blocks of this shape resident; *smem = the block's
+// dynamic shared memory with it.
+uint32_t fit_heap_snodes(gastar_ctx* c, uint32_t kinds, uint32_t warps, uint32_t ew, bool multi, uint32_t threads,
+                         int blocks_per_sm, size_t* smem, bool buckets = false);
 int occupancy_blocks(struct ::gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem);
 int device_min_weight(struct ::gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStream_t st,
                       uint32_t* out);
@@ -68,7 +73,7 @@ struct gastar_ctx {
     char name[256] = {0};
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    gastar::DevBuf table, dense, touched, heaps, hdr, stage, desc, ctl, team, path, misc, weights;
+    gastar::DevBuf table, dense, touched, heaps, hdr, stage, desc, ctl, team, path, misc, weights, buckets;
     bool table_dirty = true;       // hash table needs a full clear before the next solve
     uint32_t prev_slot_words = 2;  // slot width of the solve that filled the touched list
     uint64_t launches = 0;         // kernels launched by this context

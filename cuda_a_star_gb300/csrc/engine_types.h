@@ -97,7 +97,17 @@ struct alignas(16) InstDesc {
     uint64_t touched_cap;
     uint32_t prev_slot_words, pad1;
     uint64_t start_hi[2], goal_hi[2];  // key words 2..3 (generic plugin states)
+    // Bucket front of the open list (bq_pages == 0 -> heaps only): per warp
+    // bq_pages pages of 32 entries at bq_base, then the heaps' page links
+    // (heaps * bq_pages words), then their free-page stacks (as many words).
+    void* bq_base;
+    uint32_t bq_pages, pad2;
 };
+
+// Bytes of an instance's bucket area.
+inline __host__ __device__ size_t bucket_area_bytes(uint32_t heaps, uint32_t pages, uint32_t entry_bytes) {
+    return (size_t)heaps * pages * (32 * (size_t)entry_bytes + 8);
+}
 
 // Per-iteration state of a one-block team (shared memory); iteration t uses
 // slot t % kSlots.
@@ -153,7 +163,7 @@ struct LaunchParams {
     uint32_t* next;           // work counter for single-block teams
     uint32_t team_ctas;       // 1 = one block per instance; >1 = all blocks on instance 0
     uint32_t heap_snodes;     // shared-memory heap nodes per warp + 1 (0 = kHeapSmemNodes)
-    uint32_t bucket_pages;    // shared-memory bucket pages per warp (0 = heap only)
+    uint32_t buckets;         // 1 = blocks carry the bucket push scratch (some instance has buckets)
     uint32_t pad2;
     TeamCtl* team;            // multi-block team control (device)
     void* stage;              // multi-block stage buffer (device)

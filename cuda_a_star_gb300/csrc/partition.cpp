@@ -10,7 +10,6 @@
 namespace gastar {
 
 namespace {
-constexpr uint32_t kHeapSmemNodesHost = 7;  // must match kHeapSmemNodes (device)
 }
 
 bool make_sliding_problem(uint32_t n, const uint8_t* start, const uint8_t* goal, uint32_t heuristic,
@@ -71,11 +70,16 @@ PartPlan plan_partition(const Problem& p, const PartConfig& c) {
         pl.path_words = (512ull * key_words(p.kind)) << c.retry_level;
     }
     const uint64_t per_heap = (entries + c.warps - 1) / c.warps;
-    pl.heap_cap = (uint32_t)std::max<uint64_t>(2 * kHeapSmemNodesHost, (per_heap * 2 + 31) / 32);
+    pl.heap_cap = (uint32_t)std::max<uint64_t>(2 * c.heap_snodes, (per_heap * 2 + 31) / 32);
     const uint64_t hdr_end = table_bytes + (uint64_t)c.warps * 8;
     pl.heap_off = (hdr_end + 255) & ~255ull;
     const uint64_t heap_bytes = (uint64_t)c.warps * (pl.heap_cap + 1) * 32 * entry_bytes(p.kind);
     uint64_t end = pl.heap_off + heap_bytes;
+    if (c.buckets) {  // as many pages per warp as the heap has nodes
+        pl.bq_pages = pl.heap_cap;
+        pl.bq_off = (end + 255) & ~255ull;
+        end = pl.bq_off + bucket_area_bytes(c.warps, pl.bq_pages, entry_bytes(p.kind));
+    }
     if (p.kind == KIND_GRID && c.own_weights) {
         pl.weights_off = (end + 255) & ~255ull;
         end = pl.weights_off + (uint64_t)p.W * p.H;
@@ -107,6 +111,10 @@ void fill_desc(InstDesc& d, const Problem& p, const PartConfig& c, const PartPla
     d.heaps = c.warps;
     d.heap_hdr = reinterpret_cast<uint32_t*>(base + pl.table_words * 8);
     d.heap_nodes = base + pl.heap_off;
+    if (pl.bq_pages) {
+        d.bq_base = base + pl.bq_off;
+        d.bq_pages = pl.bq_pages;
+    }
     d.heap_cap = pl.heap_cap;
     d.ew = c.ew;
     d.max_exp = c.max_exp;

@@ -28,14 +28,18 @@ struct PartConfig {
     uint64_t max_exp = 0;
     uint32_t timeout_ms = 0;
     uint32_t retry_level = 0;     // capacities scale by 4^retry_level
+    uint32_t heap_snodes = kHeapSmemNodes;  // heap nodes below this index live in shared memory
+    bool buckets = false;         // bucket front in front of the warp-heaps
     bool own_weights = false;     // grid weights live inside the partition
 };
 
-// Byte layout of one partition: table | heap headers | heap nodes | weights.
+// Byte layout of one partition: table | heap headers | heap nodes | bucket area | weights.
 struct PartPlan {
     uint64_t table_words = 0, table_mask = 0, table_limit = 0;
     uint32_t heap_cap = 0;
     uint64_t heap_off = 0, weights_off = 0, bytes = 0;
+    uint64_t bq_off = 0;          // bucket area (pages, links, free stacks)
+    uint32_t bq_pages = 0;        // pages per warp (0 = no buckets)
     uint64_t path_words = 0;      // path-arena share
 };
 

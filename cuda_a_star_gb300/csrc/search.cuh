@@ -463,19 +463,19 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     hp.snodes = snodes_all + (size_t)warp * (hp.sn - 1) * 32;
     hp.hdr = d.heap_hdr + 2 * hid;
     hp.cap = d.heap_cap;
-    // Shared memory after the heap nodes: every warp's bucket pages, then the
-    // push scratch words, the page links and the free-page stacks.
+    // Bucket front: pages, links and free stacks in the instance's bucket
+    // area; the push scratch (64 words per warp) in shared memory after the
+    // heap nodes.
     Buckets<KW> bq;
     {
-        const uint32_t BP = P.bucket_pages;
-        E* const pages_all = snodes_all + (size_t)W * (hp.sn - 1) * 32;
-        uint32_t* const upd_all = reinterpret_cast<uint32_t*>(pages_all + (size_t)W * BP * 32);
-        uint16_t* const link_all = reinterpret_cast<uint16_t*>(upd_all + (size_t)W * 32);
+        const uint32_t BP = P.buckets ? d.bq_pages : 0u;
+        E* const pages_all = reinterpret_cast<E*>(d.bq_base);
+        uint32_t* const link_all = reinterpret_cast<uint32_t*>(pages_all + (size_t)H * BP * 32);
         bq.P = BP;
-        bq.pages = pages_all + (size_t)warp * BP * 32;
-        bq.upd = upd_all + (size_t)warp * 32;
-        bq.link = link_all + (size_t)warp * BP;
-        bq.fstack = link_all + (size_t)W * BP + (size_t)warp * BP;
+        bq.pages = pages_all + (size_t)hid * BP * 32;
+        bq.link = link_all + (size_t)hid * BP;
+        bq.fstack = link_all + (size_t)H * BP + (size_t)hid * BP;
+        bq.upd = reinterpret_cast<uint32_t*>(snodes_all + (size_t)W * (hp.sn - 1) * 32) + (size_t)warp * 64;
         bq_init(bq, lane);
     }
 
@@ -1049,13 +1049,11 @@ __device__ __forceinline__ void dispatch(const LaunchParams& P, CtaShared& sm, c
 //  * plain (team_ctas > 1): every block works on instance 0 (cooperative launch);
 //  * batch/serve: blocks of the heavy teams first take heavy instances together,
 //    then every block takes instances one block each from a work counter.
-// The batch/serve kernel (all kinds) runs up to 16 warps per block; the
-// one-kind kernels of the plain engine run at most 8, which leaves them twice
-// the registers.
-constexpr int max_threads_for(uint32_t kinds) { return kinds == kKindsAll ? 512 : 256; }
-
-template <uint32_t KINDS>
-__global__ void __launch_bounds__(max_threads_for(KINDS), 1) search_kernel(LaunchParams P) {
+// MAXT bounds the block size: 256 threads (8 warps) leave the compiler up to
+// 255 registers per thread, no spills; the all-kinds kernel has a second
+// instantiation for 16-warp blocks (batch/serve), capped at 128 registers.
+template <uint32_t KINDS, int MAXT = 256>
+__global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
     __shared__ CtaShared sm;
     if (P.team_ctas > 1) {
         if (threadIdx.x == 0) sm.desc = P.insts[0];

@@ -97,6 +97,7 @@ struct gastar_server {
     DevBuf arena, descs, ctls, order, counters, path_descs, path_arena, team_ctl, team_stage;
     uint32_t heavy_teams = 0;
     uint64_t heavy_stage_bytes = 0;
+    uint32_t heap_snodes = kHeapSmemNodes;  // shared-memory heap nodes per warp
     RangeAlloc alloc;
     uint32_t max_active = 0, threads = 0;
     size_t smem = 0;
@@ -125,6 +126,7 @@ PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool 
     pc.sliding_states = s->cfg.sliding_states;
     pc.retry_level = retry_level;
     pc.own_weights = true;
+    pc.heap_snodes = s->heap_snodes;
     return pc;
 }
 
@@ -251,6 +253,8 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
         delete s;
         return nullptr;
     }
+    s->heap_snodes = fit_heap_snodes(c, kKindsAll, cf.warps_per_block, cf.expansion_width, false, s->threads, nb,
+                                     &s->smem);
     const uint32_t resident = (uint32_t)(nb * c->sms);
     s->max_active = cf.max_active ? cf.max_active : resident;
     const uint32_t m = s->max_active;
@@ -350,6 +354,7 @@ int gastar_serve_step(gastar_server* s) {
     std::memset(&P, 0, sizeof(P));
     P.insts = reinterpret_cast<const InstDesc*>(s->descs.p);
     P.n_insts = (uint32_t)light.size();
+    P.heap_snodes = s->heap_snodes;
     P.order = reinterpret_cast<const uint32_t*>(s->order.p);
     P.next = reinterpret_cast<uint32_t*>(s->counters.p);
     P.team_ctas = 1;

@@ -162,6 +162,9 @@ typedef struct gastar_batch_config {
     uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
     uint64_t promote_expansions; /* puzzles past this many expansions are re-solved by the
                                     plain engine on the whole GPU (0 = never) */
+    uint32_t open_list;        /* 0 = warp-heaps; 1 = f-buckets (pages in the partition)
+                                  in front of the warp-heaps */
+    uint32_t pad;
 } gastar_batch_config;
 
 void gastar_batch_config_default(gastar_batch_config *cfg);
@@ -192,6 +195,11 @@ int gastar_batch_autotune(gastar_batch *b, uint32_t sample, const char *cache_pa
 /* Device time of the last run's kernel(s) and the bytes copied each way. */
 int gastar_batch_stats(gastar_batch *b, float *kernel_ms, uint64_t *h2d_bytes,
                        uint64_t *d2h_bytes, uint64_t *device_bytes);
+/* Kernel time of the last run by phase: the persistent launch, the re-run of
+ * overflowed instances with larger partitions, and the plain-engine re-solves
+ * of promoted puzzles; with how many instances took the last two. */
+int gastar_batch_phases(gastar_batch *b, float *main_ms, float *retry_ms, float *promote_ms,
+                        uint32_t *retried, uint32_t *promoted);
 
 /* ---- served GA*: continuous batching of solve requests ----
  * No reference counterpart (one instance per process there).  Requests wait in

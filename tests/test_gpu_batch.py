@@ -5,8 +5,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_mixed_batch_matches_oracle(engine, oracle, gastar):
-    b = engine.batch(warps_per_block=8, expansion_width=32)
+@pytest.mark.parametrize("open_list", [0, 1])
+def test_mixed_batch_matches_oracle(engine, oracle, gastar, open_list):
+    b = engine.batch(warps_per_block=8, expansion_width=32, open_list=open_list)
     cases = []
     for i in range(24):
         s, g = gastar.gen_sliding(4, 500 + i, 20, 50)
@@ -59,14 +60,21 @@ def test_batch_equals_plain(engine, gastar):
     b.close()
 
 
-def test_batch_partition_overflow_is_retried(engine, oracle, gastar):
-    """Partitions sized far below the need overflow; the instances are
-    re-solved with larger partitions and still match the oracle."""
-    b = engine.batch(warps_per_block=4, expansion_width=32, sliding_states=4096)
-    inst = [gastar.gen_sliding(4, 1300 + i, 25, 40) for i in range(6)]
+@pytest.mark.parametrize("count", [6, 70])
+def test_batch_partition_overflow_is_retried(engine, oracle, gastar, count):
+    """Partitions sized far below the need overflow.  A few overflowed
+    instances are re-solved by the plain engine; many go through a second
+    batch launch with larger partitions first.  All still match the oracle."""
+    b = engine.batch(warps_per_block=4, expansion_width=32, sliding_states=2048)
+    inst = [gastar.gen_sliding(4, 1300 + i, 25, 40) for i in range(count)]
     for s, g in inst:
         b.add_sliding(s, g)
     b.run()
+    st = b.stats()
+    if count <= 64:
+        assert st["retried"] == 0 and st["promoted"] > 0
+    else:
+        assert st["retried"] > 64
     for i, (s, g) in enumerate(inst):
         r = b.result(i)
         o, _ = oracle.sliding_astar(4, s, g, path=False)
