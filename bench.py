@@ -150,11 +150,11 @@ def run_batched(g, eng, steps: int) -> dict:
     build_dir = os.path.join(ROOT, "cuda_a_star_gb300", "_build")
     cache = os.path.join(build_dir, "autotune_cache.txt") if os.path.isdir(build_dir) else None
     t0 = time.perf_counter()
-    tuned = tuner.autotune(sample=64, cache_path=cache)
+    tuned = tuner.autotune(sample=128, cache_path=cache)
     tune_s = time.perf_counter() - t0
     tuner.close()
     cfgkw = {k: tuned[k] for k in ("warps_per_block", "expansion_width", "load_factor",
-                                    "delta_grid", "heavy_team", "open_list")}
+                                    "delta_grid", "heavy_team", "heavy_cells", "open_list")}
     # end to end: host buffers -> upload -> solve -> results and paths back
     t0 = time.perf_counter()
     b = eng.batch(**cfgkw)

@@ -233,7 +233,8 @@ class Batch:
         self.cfg = out
         return {"warps_per_block": out.warps_per_block, "expansion_width": out.expansion_width,
                 "load_factor": round(out.load_factor, 3), "delta_grid": out.delta_grid,
-                "heavy_team": out.heavy_team, "open_list": out.open_list, "trial_ms": ms.value}
+                "heavy_team": out.heavy_team, "heavy_cells": out.heavy_cells,
+                "open_list": out.open_list, "trial_ms": ms.value}
 
     def run(self) -> None:
         _check(lib().gastar_batch_run(self._h), "gastar_batch_run")

@@ -72,6 +72,7 @@ struct gastar_batch {
     float main_ms = 0, retry_ms = 0, promote_ms = 0;  // kernel time by phase of the last run
     uint32_t retry_level = 0;   // partitions scale by 4^retry_level
     uint32_t retried = 0;       // instances re-solved with larger partitions in the last run
+    double block_share = 0;     // > 0: use this share of the resident blocks (autotuner trials)
     bool uploaded = false;
     DevBuf arena, weights, descs, ctls, order, counters, paths;
     std::vector<InstDesc> h_desc;
@@ -206,6 +207,8 @@ int batch_upload(gastar_batch* b) {
     b->heap_snodes = fit_heap_snodes(c, present, pc.warps, pc.ew, false, b->threads, nb, &b->smem, pc.buckets);
     pc.heap_snodes = b->heap_snodes;
     b->blocks = b->cfg.blocks ? b->cfg.blocks : (uint32_t)(nb * c->sms);
+    if (b->block_share > 0)
+        b->blocks = std::max(1u, (uint32_t)((double)nb * c->sms * b->block_share + 0.5));
     b->blocks = std::max(1u, std::min(b->blocks, n));
 
     // Heavy instances (large grids) are solved by teams of heavy_team blocks;
@@ -669,9 +672,11 @@ bool cache_lookup(const char* path, const std::string& sig, gastar_batch_config&
         unsigned w, ew, dg, team;
         float lf;
         unsigned ol = 0;
-        const int got = std::sscanf(line, "%599s %u %u %f %u %u %u", key, &w, &ew, &lf, &dg, &team, &ol);
+        unsigned long long hc = 0;
+        const int got = std::sscanf(line, "%599s %u %u %f %u %u %u %llu", key, &w, &ew, &lf, &dg, &team, &ol, &hc);
         if (got >= 6 && sig == key) {
-            cfg.open_list = got == 7 ? ol : 0;
+            cfg.open_list = got >= 7 ? ol : 0;
+            if (got == 8 && hc) cfg.heavy_cells = hc;
             cfg.warps_per_block = w;
             cfg.expansion_width = ew;
             cfg.load_factor = lf;
@@ -685,10 +690,14 @@ bool cache_lookup(const char* path, const std::string& sig, gastar_batch_config&
 }
 
 // Device time of one trial batch over `idx` with configuration `cfg`.
+// The sample runs on the same share of the GPU as it is of the batch, so
+// that blocks per instance -- which decides whether teams pay -- match the
+// full run.
 int trial(gastar_batch* b, const std::vector<uint32_t>& idx, const gastar_batch_config& cfg, float& ms) {
     gastar_batch* t = gastar_batch_create(b->ctx, &cfg);
     if (!t) return GASTAR_OUT_OF_MEMORY;
     t->cfg.use_graph = 0;
+    t->block_share = std::min(1.0, (double)idx.size() / (double)b->insts.size());
     for (uint32_t i : idx) t->insts.push_back(b->insts[i]);
     const int rc = gastar_batch_run(t);
     ms = t->kernel_ms;
@@ -759,14 +768,19 @@ extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const cha
     if (heavy && (rc = try_values([](gastar_batch_config& c, double v) { c.heavy_team = (uint32_t)v; },
                                   {1, 2, 4, 8})) != GASTAR_OK)
         return rc;
+    if (heavy && best.heavy_team > 1 &&
+        (rc = try_values([](gastar_batch_config& c, double v) { c.heavy_cells = (uint64_t)v; },
+                         {(double)(1u << 20), (double)(1u << 21), (double)(1u << 22)})) != GASTAR_OK)
+        return rc;
     if ((rc = try_values([](gastar_batch_config& c, double v) { c.load_factor = (float)v; },
                          {0.5, 0.7, 0.85})) != GASTAR_OK)
         return rc;
     b->cfg = best;
     if (cache_path) {
         if (FILE* f = std::fopen(cache_path, "a")) {
-            std::fprintf(f, "%s %u %u %.3f %u %u %u\n", sig.c_str(), best.warps_per_block, best.expansion_width,
-                         best.load_factor, best.delta_grid, best.heavy_team, best.open_list);
+            std::fprintf(f, "%s %u %u %.3f %u %u %u %llu\n", sig.c_str(), best.warps_per_block, best.expansion_width,
+                         best.load_factor, best.delta_grid, best.heavy_team, best.open_list,
+                         (unsigned long long)best.heavy_cells);
             std::fclose(f);
         }
     }
