@@ -173,6 +173,7 @@ def run_batched(g, eng, steps: int) -> dict:
     n = len(res)
     ok = sum(1 for r in res if r.status == g.OK)
     exp = sum(r.expansions for r in res)
+    alg = sum(16 * (r.expansions + r.stale) + 32 * r.generated + 48 * r.pushes for r in res)
     ms = statistics.median(kms)
     lat = sorted(r.kernel_ms for r in res)
     b.close()
@@ -198,6 +199,9 @@ def run_batched(g, eng, steps: int) -> dict:
         "autotuned": cfgkw, "autotune_s": tune_s,
         "last_step_phases_ms": {k: phases[k] for k in ("main_ms", "retry_ms", "promote_ms",
                                                        "retried", "promoted")} if phases else None,
+        # Algorithmic bytes (16 B/pop + 32 B/generated + 48 B/pushed) over the
+        # step's kernel time, against the measured random-access peak.
+        "algorithmic_gbs": alg / (ms / 1000.0) / 1e9,
         "plain_same_mix_solves_per_s": plain_sps,
         "plain_sample": f"{len(sample)} instances (every 16th of each class), one per launch",
         "batched_over_plain": (n / (ms / 1000.0)) / plain_sps,
@@ -443,6 +447,9 @@ def run_ours(args) -> dict:
         out["optimal_cost_agreement"] = agree
     if rank == 0 and world == 1 and not args.no_batched:
         out["batched"] = run_batched(g, eng, max(1, min(args.steps, 3)))
+        ra = out["roofline"].get("random_access", {})
+        if ra.get("gather_gbs"):
+            out["batched"]["frac_of_random_gather"] = out["batched"]["algorithmic_gbs"] / ra["gather_gbs"]
     if rank == 0 and world == 1 and not args.no_served:
         out["served"] = run_served(g, eng)
     if world > 1:
