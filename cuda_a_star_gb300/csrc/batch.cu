@@ -91,16 +91,18 @@ extern "C" {
 
 void gastar_batch_config_default(gastar_batch_config* cfg) {
     std::memset(cfg, 0, sizeof(*cfg));
-    cfg->warps_per_block = 8;
+    // The autotuner's usual choice on mixed puzzle/grid batches.
+    cfg->warps_per_block = 16;
     cfg->expansion_width = 32;
-    cfg->load_factor = 0.75f;
+    cfg->load_factor = 0.5f;
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
     cfg->use_graph = 1;
-    cfg->delta_grid = 36;
-    cfg->heavy_team = 4;
-    cfg->heavy_cells = 1ull << 20;
+    cfg->delta_grid = 18;
+    cfg->heavy_team = 2;
+    cfg->heavy_cells = 1ull << 21;
     cfg->promote_expansions = 1ull << 21;
+    cfg->open_list = 1;
 }
 
 gastar_batch* gastar_batch_create(gastar_ctx* c, const gastar_batch_config* cfg) {

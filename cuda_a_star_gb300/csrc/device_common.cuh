@@ -490,7 +490,8 @@ template <int KW> struct Buckets {
     Entry<KW>* pages;  // P pages of 32 entries (global memory)
     uint32_t* link;    // the page below each page in its bucket's stack (global memory)
     uint32_t* fstack;  // pages freed while the register cache was full (global memory)
-    uint32_t* upd;     // per-bucket scratch of a push (32 words, shared memory)
+    uint32_t* upd;     // per-bucket scratch of a push (64 words, shared memory)
+    uint32_t* state;   // saved state of a suspended search (global memory)
     uint32_t P;        // pages (0 = buckets off)
     uint32_t bump;     // pages >= bump were never used (warp-uniform)
     uint32_t nfs;      // entries on fstack (warp-uniform)
@@ -674,26 +675,30 @@ __device__ uint32_t open_pop(WarpHeap<KW>& h, Buckets<KW>& q, uint32_t E, uint64
     return taken;
 }
 
-// Moves every bucket entry into the heap (before the heap is saved).
-// Returns false when the heap ran full.
-template <int KW> __device__ bool open_drain(WarpHeap<KW>& h, Buckets<KW>& q, int lane) {
-    if (!q.P) return true;
-    bool ok = true;
-    for (uint32_t guard = 0; guard <= q.P; ++guard) {
-        const uint32_t mask = __ballot_sync(kFull, q.head != kNoPage);
-        if (!mask) break;
-        const int bl = __ffs(mask) - 1;
-        const uint32_t hd = __shfl_sync(kFull, q.head, bl), hc = __shfl_sync(kFull, q.hcnt, bl);
-        const uint32_t nx = __ldcg(q.link + hd);
-        const Entry<KW> x = (uint32_t)lane < hc ? ld_entry(q.pages + (size_t)hd * 32 + lane) : inf_entry<KW>();
-        if (!heap_push(h, x, hc, lane)) ok = false;
-        if (lane == bl) {
-            q.head = nx;
-            q.hcnt = nx == kNoPage ? 0u : 32u;
-        }
+// The bucket state of a suspended search stays beside its pages: lane l
+// saves its bucket's head page and count and its cached free page; lane 0
+// the window start, the never-used and free-stack counts and the cache size.
+template <int KW> __device__ __forceinline__ void bq_save(const Buckets<KW>& q, int lane) {
+    if (!q.P) return;
+    __stcg(q.state + lane, q.head);
+    __stcg(q.state + 32 + lane, q.hcnt);
+    __stcg(q.state + 64 + lane, q.cache);
+    if (lane == 0) {
+        __stcg(q.state + 96, q.lo);
+        __stcg(q.state + 97, q.bump);
+        __stcg(q.state + 98, q.nfs);
+        __stcg(q.state + 99, q.fc);
     }
-    bq_init(q, lane);
-    return ok;
+}
+template <int KW> __device__ __forceinline__ void bq_restore(Buckets<KW>& q, int lane) {
+    if (!q.P) return;
+    q.head = __ldcg(q.state + lane);
+    q.hcnt = __ldcg(q.state + 32 + lane);
+    q.cache = __ldcg(q.state + 64 + lane);
+    q.lo = __ldcg(q.state + 96);
+    q.bump = __ldcg(q.state + 97);
+    q.nfs = __ldcg(q.state + 98);
+    q.fc = __ldcg(q.state + 99);
 }
 
 // ---------------------------------------------------------------------------

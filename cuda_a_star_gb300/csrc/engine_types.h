@@ -99,14 +99,17 @@ struct alignas(16) InstDesc {
     uint64_t start_hi[2], goal_hi[2];  // key words 2..3 (generic plugin states)
     // Bucket front of the open list (bq_pages == 0 -> heaps only): per warp
     // bq_pages pages of 32 entries at bq_base, then the heaps' page links
-    // (heaps * bq_pages words), then their free-page stacks (as many words).
+    // (heaps * bq_pages words), then their free-page stacks (as many words),
+    // then each heap's saved bucket state (kBucketStateWords words).
     void* bq_base;
     uint32_t bq_pages, pad2;
 };
 
+constexpr uint32_t kBucketStateWords = 128;
+
 // Bytes of an instance's bucket area.
 inline __host__ __device__ size_t bucket_area_bytes(uint32_t heaps, uint32_t pages, uint32_t entry_bytes) {
-    return (size_t)heaps * pages * (32 * (size_t)entry_bytes + 8);
+    return (size_t)heaps * pages * (32 * (size_t)entry_bytes + 8) + (size_t)heaps * kBucketStateWords * 4;
 }
 
 // Per-iteration state of a one-block team (shared memory); iteration t uses

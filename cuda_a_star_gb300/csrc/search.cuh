@@ -475,6 +475,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         bq.pages = pages_all + (size_t)hid * BP * 32;
         bq.link = link_all + (size_t)hid * BP;
         bq.fstack = link_all + (size_t)H * BP + (size_t)hid * BP;
+        bq.state = link_all + 2 * (size_t)H * BP + (size_t)hid * kBucketStateWords;
         bq.upd = reinterpret_cast<uint32_t*>(snodes_all + (size_t)W * (hp.sn - 1) * 32) + (size_t)warp * 64;
         bq_init(bq, lane);
     }
@@ -534,6 +535,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         have_prev = true;  // the start is the only open entry; every slot starts empty
     } else {
         heap_restore(hp, lane);
+        bq_restore(bq, lane);
         best_r = ld_vol(&ctl->best);
         have_prev = false;
     }
@@ -967,11 +969,6 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             for (int i = 0; i < 5; ++i) sm.cnt[i] = 0;
         }
     }
-    if (status == kInf && bq.P) {  // suspending: the buckets go back into the heap
-        if (!open_drain(hp, bq, lane) && lane == 0) atomicCAS(&sm.agg_err_prev, 0u, (uint32_t)ST_HEAP_FULL);
-        __syncthreads();
-        if (!multi && sm.agg_err_prev) status = ST_HEAP_FULL;
-    }
     if (status == kInf) {
         // Suspending: fold in what the iterations not tested yet found -- a
         // goal popped there is in no heap any more -- and stop on entries
@@ -1007,6 +1004,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     }
     if (status == kInf) {  // suspended: keep the search state resident
         heap_save(hp, lane);
+        bq_save(bq, lane);
         if (leader) {
             ctl->best = best_r;
             ctl->iterations = it0 + it;

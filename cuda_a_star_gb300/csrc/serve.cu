@@ -127,6 +127,7 @@ PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool 
     pc.retry_level = retry_level;
     pc.own_weights = true;
     pc.heap_snodes = s->heap_snodes;
+    pc.buckets = s->cfg.open_list == 1;
     return pc;
 }
 
@@ -220,6 +221,7 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     c->delta_grid = 18;
     c->heavy_team = 4;
     c->heavy_cells = 1ull << 20;
+    c->open_list = 1;
 }
 
 gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
@@ -242,7 +244,8 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
     budget = std::min<uint64_t>(budget, free_b > (2ull << 30) ? free_b - (2ull << 30) : free_b / 2);
     cf.budget_bytes = budget;
     s->threads = cf.warps_per_block * 32;
-    s->smem = block_smem_bytes(kKindsAll, cf.warps_per_block, cf.expansion_width, false);
+    const bool buckets = cf.open_list == 1;
+    s->smem = block_smem_bytes(kKindsAll, cf.warps_per_block, cf.expansion_width, false, kHeapSmemNodes, buckets);
     if (s->smem + 4096 > c->smem_optin) {  // + the kernel's static shared memory
         set_error("serve: warps_per_block x expansion_width needs more shared memory than a block has");
         delete s;
@@ -254,7 +257,7 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
         return nullptr;
     }
     s->heap_snodes = fit_heap_snodes(c, kKindsAll, cf.warps_per_block, cf.expansion_width, false, s->threads, nb,
-                                     &s->smem);
+                                     &s->smem, buckets);
     const uint32_t resident = (uint32_t)(nb * c->sms);
     s->max_active = cf.max_active ? cf.max_active : resident;
     const uint32_t m = s->max_active;
@@ -355,6 +358,7 @@ int gastar_serve_step(gastar_server* s) {
     P.insts = reinterpret_cast<const InstDesc*>(s->descs.p);
     P.n_insts = (uint32_t)light.size();
     P.heap_snodes = s->heap_snodes;
+    P.buckets = s->cfg.open_list == 1 ? 1u : 0u;
     P.order = reinterpret_cast<const uint32_t*>(s->order.p);
     P.next = reinterpret_cast<uint32_t*>(s->counters.p);
     P.team_ctas = 1;

@@ -162,8 +162,8 @@ typedef struct gastar_batch_config {
     uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
     uint64_t promote_expansions; /* puzzles past this many expansions are re-solved by the
                                     plain engine on the whole GPU (0 = never) */
-    uint32_t open_list;        /* 0 = warp-heaps; 1 = f-buckets (pages in the partition)
-                                  in front of the warp-heaps */
+    uint32_t open_list;        /* 0 = warp-heaps; 1 (default) = f-buckets (pages in the
+                                  partition) in front of the warp-heaps */
     uint32_t pad;
 } gastar_batch_config;
 
@@ -222,6 +222,10 @@ typedef struct gastar_serve_config {
     uint32_t heavy_team;       /* blocks per team for heavy requests (1 = no teams) */
     uint32_t heavy_teams;      /* teams per launch (0 = a quarter of the resident blocks) */
     uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
+    uint32_t open_list;        /* 0 = warp-heaps; 1 (default) = f-buckets (pages in the
+                                  partition, state kept there between steps) in front of
+                                  the warp-heaps */
+    uint32_t pad;
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);

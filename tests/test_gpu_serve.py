@@ -39,9 +39,12 @@ def _check(oracle, r, res):
         assert oracle.grid_validate(r[1], r[2], r[3], res.path) == (True, res.cost)
 
 
-def test_results_same_alone_and_in_mix(engine, oracle, gastar):
+@pytest.mark.parametrize("open_list", [0, 1])
+def test_results_same_alone_and_in_mix(engine, oracle, gastar, open_list):
+    """Requests suspended every 16 iterations (heaps, or buckets whose state is
+    kept beside their pages) match the oracle, alone and in the mix."""
     reqs = _mix(gastar, 24)
-    srv = engine.server(slice_iters=16, budget_bytes=8 << 30)
+    srv = engine.server(slice_iters=16, budget_bytes=8 << 30, open_list=open_list)
     # Staggered arrivals: a third before the first step, the rest while running.
     ids = [_submit(srv, r) for r in reqs[:8]]
     srv.step()
@@ -54,7 +57,7 @@ def test_results_same_alone_and_in_mix(engine, oracle, gastar):
         _check(oracle, r, mixed[i])
     # The same requests one at a time.
     for r, i in zip(reqs, ids):
-        one = engine.server(slice_iters=16, budget_bytes=2 << 30)
+        one = engine.server(slice_iters=16, budget_bytes=2 << 30, open_list=open_list)
         j = _submit(one, r)
         alone = one.drain([j])[j]
         one.close()
