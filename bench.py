@@ -49,10 +49,29 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _instances(g):
+def _instances(g, rank: int = 0):
+    """The workload's instances; replica rank r gets its own seeds."""
     n = WORKLOAD["n"]
     lo, hi = WORKLOAD["walk"]
-    return [g.gen_sliding(n, WORKLOAD["seed0"] + i, lo, hi) for i in range(WORKLOAD["instances"])]
+    base = WORKLOAD["seed0"] + rank * 1_000_000
+    return [g.gen_sliding(n, base + i, lo, hi) for i in range(WORKLOAD["instances"])]
+
+
+def _job_ms(local_ms: float, world: int) -> float:
+    """The job's timed duration: the maximum over the ranks' timed regions."""
+    if world == 1:
+        return local_ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _job_value(units_per_rank: int, steps: int, world: int, job_ms: float) -> float:
+    """Whole-job throughput: the units all ranks processed / the job's time."""
+    return units_per_rank * steps * world / (job_ms / 1000.0)
 
 
 def _oracle_run(insts, threads=0):
@@ -334,7 +353,7 @@ def run_ours(args) -> dict:
     stream = torch.cuda.current_stream()
     cfg = g.make_config(num_queues=WORKLOAD["num_queues"], table_log2=WORKLOAD["table_log2"],
                         stream=stream.cuda_stream)
-    insts = _instances(g)
+    insts = _instances(g, rank)  # replicas: every rank its own 64 instances
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
     def step(collect):
@@ -367,6 +386,8 @@ def run_ours(args) -> dict:
         results.extend(rs)
     clk = clocks.stop()
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     # --- end-to-end steps through the C ABI with host buffers ---
     e2e_s, h2d, d2h = [], 0, 0
     for k in range(args.steps):
@@ -378,14 +399,9 @@ def run_ours(args) -> dict:
         e2e_s.append(time.perf_counter() - t0)
         h2d = sum(r.h2d_bytes for r in rs)
         d2h = sum(r.d2h_bytes for r in rs)
-    ms = max(step_ms) if world == 1 else None
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _job_ms(sum(step_ms), world)
     n_inst = WORKLOAD["instances"]
-    value = n_inst * args.steps * world / (total_ms / 1000.0)
+    value = _job_value(n_inst, args.steps, world, total_ms)
     exp = sum(r.expansions for r in results)
     lat = sorted(r.total_ms for r in results)
     kern_s = sum(r.kernel_ms for r in results) / 1000.0
