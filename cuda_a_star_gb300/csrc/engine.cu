@@ -687,9 +687,7 @@ int gastar_solve_grid(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weig
     }
     if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
     const size_t cells = (size_t)w * h;
-    uint32_t minw = 255;
-    for (size_t i = 0; i < cells; ++i)
-        if (weights[i] && weights[i] < minw) minw = weights[i];
+    const uint32_t minw = min_passable_weight(weights, (size_t)w * h);
     gastar_config dc;
     gastar_config_default(&dc);
     cudaStream_t st = (cfg && cfg->stream) ? (cudaStream_t)cfg->stream : c->stream;

@@ -60,6 +60,8 @@ uint32_t sliding_h(uint32_t n, const uint8_t* b, const uint8_t* goal, uint32_t h
 bool sliding_solvable(uint32_t n, const uint8_t* s, const uint8_t* g);
 uint32_t grid_h(uint32_t x, uint32_t y, uint32_t tx, uint32_t ty, uint32_t minw, uint32_t heuristic);
 uint64_t next_pow2(uint64_t v);
+// Least non-zero weight of a grid, 255 if none (vectorised scan).
+uint8_t min_passable_weight(const uint8_t* weights, size_t cells);
 
 }  // namespace gastar
 

@@ -219,7 +219,7 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     c->expansion_width = 32;
     c->load_factor = 0.75f;
     c->delta_grid = 18;
-    c->heavy_team = 4;
+    c->heavy_team = 8;  // the largest grids (8192^2) bound the tail latency
     c->heavy_cells = 1ull << 20;
     c->open_list = 1;
 }

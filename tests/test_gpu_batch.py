@@ -65,7 +65,7 @@ def test_batch_partition_overflow_is_retried(engine, oracle, gastar, count):
     """Partitions sized far below the need overflow.  A few overflowed
     instances are re-solved by the plain engine; many go through a second
     batch launch with larger partitions first.  All still match the oracle."""
-    b = engine.batch(warps_per_block=4, expansion_width=32, sliding_states=2048)
+    b = engine.batch(warps_per_block=4, expansion_width=32, load_factor=0.75, sliding_states=256)
     inst = [gastar.gen_sliding(4, 1300 + i, 25, 40) for i in range(count)]
     for s, g in inst:
         b.add_sliding(s, g)
