@@ -131,3 +131,10 @@ def test_cli_end_to_end(gastar, oracle, tmp_path):
     cells = [tuple(map(int, l.split(","))) for l in lines[1:]]
     o, _ = oracle.grid_astar(wts, (0, 0), (59, 39), path=False)
     assert oracle.grid_validate(wts, (0, 0), (59, 39), [y * 60 + x for x, y in cells]) == (True, o.cost)
+    # The same grid from the binary dense format.
+    binf, out2 = tmp_path / "g.bin", tmp_path / "out2.txt"
+    binf.write_bytes(gastar.encode_grid_binary(wts, (0, 0), (59, 39)))
+    subprocess.run([CLI, "--version", "pathfinding", "--input-format", "binary", "--input-data", str(binf),
+                    "--output-data", str(out2), "--delta", "18"], check=True)
+    cells2 = [tuple(map(int, l.split(","))) for l in out2.read_text().split()[1:]]
+    assert oracle.grid_validate(wts, (0, 0), (59, 39), [y * 60 + x for x, y in cells2]) == (True, o.cost)
