@@ -208,7 +208,10 @@ struct GridDom {
     static constexpr int MAXN = 8;
     using KeyT = uint64_t;
     using Tab = DenseTab;
-    struct Pre { int x, y; };
+    struct Pre {
+        int x, y;
+        uint64_t wts;  // byte m: weight of the cell move m enters (0 = obstacle or off the board)
+    };
 
     struct Ctx {
         const uint8_t* w;
@@ -270,9 +273,18 @@ struct GridDom {
     }
     static __device__ __forceinline__ bool is_goal(const Ctx& c, KeyT k) { return k == c.goal; }
     static __device__ __forceinline__ bool is_start(const Ctx& c, KeyT k) { return k == c.start; }
+    // The eight neighbours' weights load together, before any successor
+    // needs one (every load is inside the board, whatever k holds).
     static __device__ __forceinline__ Pre prepare(const Ctx& c, KeyT k) {
         const uint32_t cell = (uint32_t)k;
-        return Pre{(int)(cell % c.W), (int)(cell / c.W)};
+        Pre p{(int)(cell % c.W), (int)(cell / c.W), 0};
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int nx = p.x + dx(m), ny = p.y + dy(m);
+            if (nx >= 0 && ny >= 0 && nx < (int)c.W && ny < (int)c.H)
+                p.wts |= (uint64_t)__ldg(c.w + (uint32_t)ny * c.W + (uint32_t)nx) << (8 * m);
+        }
+        return p;
     }
     static __device__ __forceinline__ uint32_t heur(const Ctx& c, int x, int y) {
         // 0: Chebyshev x min weight (admissible); 1: Manhattan (the reference's,
@@ -286,11 +298,10 @@ struct GridDom {
                                                 uint32_t g, uint32_t, KeyT& nk, uint32_t& ng,
                                                 uint32_t& nh) {
         if (pm != kRootMove && (uint32_t)m == inv(pm)) return false;
+        const uint32_t wt = (uint32_t)(p.wts >> (8 * m)) & 0xffu;
+        if (!wt) return false;  // obstacle or off the board
         const int nx = p.x + dx(m), ny = p.y + dy(m);
-        if (nx < 0 || ny < 0 || nx >= (int)c.W || ny >= (int)c.H) return false;
         const uint32_t cell = (uint32_t)ny * c.W + (uint32_t)nx;
-        const uint32_t wt = __ldg(c.w + cell);
-        if (!wt) return false;
         nk = cell;
         ng = g + wt;
         nh = heur(c, nx, ny);
