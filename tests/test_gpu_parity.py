@@ -13,8 +13,8 @@ def _check_sliding(oracle, n, s, g, r, heuristic=0, ref_moves=0):
     assert r.status_name == "OK", r
     if heuristic == 0:
         assert r.cost == o.cost
-    else:  # an inadmissible heuristic: valid path, never below the optimum
-        opt, _ = oracle.sliding_astar(n, s, g, heuristic=2, ref_moves=ref_moves, path=False)
+    else:  # an inadmissible heuristic: valid path, never below the optimum (admissible A*)
+        opt, _ = oracle.sliding_astar(n, s, g, heuristic=0, ref_moves=ref_moves, path=False)
         assert r.cost >= opt.cost
     ok, cost = oracle.sliding_validate(n, s, g, r.path, ref_moves=ref_moves)
     assert ok and cost == r.cost and len(r.path) == r.cost + 1
@@ -80,6 +80,20 @@ def test_sliding_edge_cases(engine, oracle, gastar):
     s, g = gastar.gen_sliding(4, 77, 60, 60)
     r = engine.solve_sliding(s, g, 4, num_queues=256, max_expansions=50, regrow=0)
     assert r.status_name == "BUDGET"
+
+
+def test_device_deadline_and_heap_capacity(engine, oracle, gastar):
+    """Limits end a search with a status and leave the context usable."""
+    s, g = gastar.gen_sliding(5, 6000, 60, 60)      # far beyond 1 ms of search
+    r = engine.solve_sliding(s, g, 5, num_queues=1024, timeout_ms=1, table_log2=26, regrow=0,
+                             path=False)
+    assert r.status_name == "TIMEOUT"
+    s2, g2 = gastar.gen_sliding(4, 6001, 20, 30)
+    _check_sliding(oracle, 4, s2, g2, engine.solve_sliding(s2, g2, 4, num_queues=4096))
+    s3, g3 = gastar.gen_sliding(4, 6002, 80, 80)    # open list far above 8 small heaps
+    r = engine.solve_sliding(s3, g3, 4, num_queues=64, heap_entries=64, regrow=0, path=False)
+    assert r.status_name == "HEAP_FULL"
+    _check_sliding(oracle, 4, s2, g2, engine.solve_sliding(s2, g2, 4, num_queues=4096))
 
 
 def test_table_regrow(engine, oracle, gastar):
