@@ -810,10 +810,10 @@ __device__ __forceinline__ Look64 tab_look_begin(const HashTab64& t, uint64_t ke
 __device__ __forceinline__ uint64_t tab_get(const HashTab64& t, uint64_t key) {
     uint64_t i = mix64(key) & t.mask;
     for (uint32_t p = 0; p < t.max_probe; ++p) {
-        const unsigned long long* ks = t.s + 2 * i;
-        unsigned long long k = __ldcg(ks);
-        if (k == key) return __ldcg(ks + 1);
-        if (k == kEmpty) return kEmpty;
+        // Key and value in one 16-byte load (they are written together).
+        const ulonglong2 kv = __ldcg(reinterpret_cast<const ulonglong2*>(t.s + 2 * i));
+        if (kv.x == key) return kv.y;
+        if (kv.x == kEmpty) return kEmpty;
         i = (i + 1) & t.mask;
     }
     return kEmpty;

@@ -22,6 +22,19 @@
 
 namespace gastar {
 
+// Launch block of a plain solve (one device allocation, one upload):
+// descriptor | control block | team control | work counter | path counter.
+constexpr size_t kLbAlign = 128;
+constexpr size_t lb_round(size_t x) { return (x + kLbAlign - 1) / kLbAlign * kLbAlign; }
+constexpr size_t kLbDesc = 0;
+constexpr size_t kLbCtl = lb_round(sizeof(InstDesc));
+constexpr size_t kLbTeam = kLbCtl + lb_round(sizeof(InstCtl));
+constexpr size_t kLbNext = kLbTeam + lb_round(sizeof(TeamCtl));
+constexpr size_t kLbUsed = kLbNext + kLbAlign;
+constexpr size_t kLbBytes = kLbUsed + kLbAlign;
+constexpr uint64_t kPathPrefixWords = 1024;   // path words read back with the control block
+constexpr uint64_t kPathArenaWords = 1 << 16;  // first path arena of a puzzle solve
+
 thread_local std::string g_last_error;
 
 void set_error(const std::string& s) { g_last_error = s; }
@@ -250,7 +263,7 @@ void gastar_config_default(gastar_config* cfg) {
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
     cfg->expansion_width = 0;  // auto
-    cfg->warps_per_block = 4;
+    cfg->warps_per_block = 0;  // auto
     cfg->load_factor = 0.75f;
     cfg->regrow = 1;
 }
@@ -283,7 +296,9 @@ gastar_ctx* gastar_create(int device) {
     if (!cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreate(&c->e0), "cudaEventCreate") ||
         !cuda_ok(cudaEventCreate(&c->e1), "cudaEventCreate") ||
-        !cuda_ok(cudaMallocHost(&c->h_ctl, sizeof(InstCtl)), "cudaMallocHost")) {
+        !cuda_ok(cudaMallocHost(&c->h_ctl, sizeof(InstCtl)), "cudaMallocHost") ||
+        !cuda_ok(cudaMallocHost(&c->h_launch, kLbBytes), "cudaMallocHost") ||
+        !cuda_ok(cudaMallocHost(reinterpret_cast<void**>(&c->h_path), kPathPrefixWords * 8), "cudaMallocHost")) {
         delete c;
         return nullptr;
     }
@@ -301,13 +316,13 @@ void gastar_destroy(gastar_ctx* c) {
     c->heaps.release();
     c->hdr.release();
     c->stage.release();
-    c->desc.release();
-    c->ctl.release();
-    c->team.release();
+    c->launch.release();
     c->path.release();
     c->misc.release();
     c->weights.release();
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->h_launch) cudaFreeHost(c->h_launch);
+    if (c->h_path) cudaFreeHost(c->h_path);
     if (c->e0) cudaEventDestroy(c->e0);
     if (c->e1) cudaEventDestroy(c->e1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -349,18 +364,22 @@ struct AttemptStats {
 
 // Runs the search (+ path rebuild) once with the given capacities.
 static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_config& cfg,
-                         uint32_t table_log2, uint64_t heap_entries, bool want_path,
+                         uint32_t table_log2, uint64_t heap_entries, std::vector<uint64_t>* path_keys,
                          cudaStream_t st, InstCtl& ctl_out, AttemptStats& as) {
+    const bool want_path = path_keys != nullptr;
     const uint32_t kinds = kind_bit(pp.kind);
     // Expansion width 0 = about 1024 warp-heaps per solve: wide enough pops
     // for large Q, enough heaps (warps) to keep the SMs busy for small Q.
     const uint32_t ew = cfg.expansion_width
                             ? std::min(32u, cfg.expansion_width)
                             : (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(8, (cfg.num_queues ? cfg.num_queues : 4096) / 1024));
-    const uint32_t W = std::min(8u, std::max(1u, cfg.warps_per_block ? cfg.warps_per_block : 4u));
-    const uint32_t threads = W * 32;
     const uint64_t Q = cfg.num_queues ? cfg.num_queues : 4096;
     uint64_t heaps = (Q + ew - 1) / ew;
+    // Warps per block 0 = 8 when that still gives at least half of the SMs a
+    // block (fewer, larger blocks: fewer parties to the hand-offs), else 4.
+    const uint32_t W = cfg.warps_per_block ? std::min(8u, cfg.warps_per_block)
+                                           : ((heaps / 8 >= (uint64_t)c->sms / 2) ? 8u : 4u);
+    const uint32_t threads = W * 32;
     uint64_t blocks = (heaps + W - 1) / W;
     const bool multi = blocks > 1;
     size_t smem = block_smem_bytes(kinds, W, ew, multi);
@@ -427,10 +446,9 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     const size_t stage_bytes = multi ? team_stage_bytes((uint32_t)blocks, W, ew, maxn, ebytes) : 16;
 
     if (!c->heaps.ensure(heap_bytes) || !c->hdr.ensure((size_t)heaps * 8) ||
-        !c->stage.ensure(stage_bytes) ||
-        !c->desc.ensure(sizeof(InstDesc)) || !c->ctl.ensure(sizeof(InstCtl)) ||
-        !c->team.ensure(sizeof(TeamCtl) + 64))
+        !c->stage.ensure(stage_bytes) || !c->launch.ensure(kLbBytes))
         return GASTAR_OUT_OF_MEMORY;
+    char* const lb = static_cast<char*>(c->launch.p);
     // Bucket front: as many pages per warp as the heap has nodes.
     if (buckets && !c->buckets.ensure(bucket_area_bytes((uint32_t)heaps, (uint32_t)cap_nodes, ebytes)))
         return GASTAR_OUT_OF_MEMORY;
@@ -464,7 +482,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     d.timeout_ns = (uint64_t)cfg.timeout_ms * 1000000ull;
     d.max_iter = cfg.max_iterations;
     d.delta = cfg.delta;
-    d.ctl = reinterpret_cast<InstCtl*>(c->ctl.p);
+    d.ctl = reinterpret_cast<InstCtl*>(lb + kLbCtl);
     if (buckets) {
         d.bq_base = c->buckets.p;
         d.bq_pages = (uint32_t)cap_nodes;
@@ -475,33 +493,47 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         d.touched_cap = touched_cap;
         d.prev_slot_words = c->prev_slot_words;
     }
-    c->h_desc = d;
-
-    team_ctl_init(c->h_team);
+    // Descriptor, zeroed control block, team control and counters: one copy.
+    char* const hl = static_cast<char*>(c->h_launch);
+    std::memset(hl, 0, kLbBytes);
+    std::memcpy(hl + kLbDesc, &d, sizeof(InstDesc));
+    team_ctl_init(*reinterpret_cast<TeamCtl*>(hl + kLbTeam));
 
     LaunchParams P;
     std::memset(&P, 0, sizeof(P));
-    P.insts = reinterpret_cast<const InstDesc*>(c->desc.p);
+    P.insts = reinterpret_cast<const InstDesc*>(lb + kLbDesc);
     P.n_insts = 1;
-    P.next = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(c->team.p) + sizeof(TeamCtl));
+    P.next = reinterpret_cast<uint32_t*>(lb + kLbNext);
     P.team_ctas = (uint32_t)blocks;
     P.heap_snodes = snodes;
     P.buckets = buckets ? 1u : 0u;
-    P.team = reinterpret_cast<TeamCtl*>(c->team.p);
+    P.team = reinterpret_cast<TeamCtl*>(lb + kLbTeam);
     P.stage = c->stage.p;
     P.barrier_timeout_ns = 2000000000ull;
 
-    GA_CUDA(cudaMemcpyAsync(c->desc.p, &c->h_desc, sizeof(InstDesc), cudaMemcpyHostToDevice, st));
-    GA_CUDA(cudaMemsetAsync(c->ctl.p, 0, sizeof(InstCtl), st));
-    GA_CUDA(cudaMemcpyAsync(c->team.p, &c->h_team, sizeof(TeamCtl), cudaMemcpyHostToDevice, st));
-    GA_CUDA(cudaMemsetAsync(P.next, 0, 16, st));
-    as.h2d += sizeof(InstDesc) + sizeof(TeamCtl);
+    GA_CUDA(cudaMemcpyAsync(lb, hl, kLbBytes, cudaMemcpyHostToDevice, st));
+    as.h2d += kLbBytes;
     GA_CUDA(cudaEventRecord(c->e0, st));
     int rc = launch_search(c, kinds, P, (uint32_t)blocks, threads, smem, st);
     if (rc != GASTAR_OK) return rc;
     ++as.launches;
     GA_CUDA(cudaEventRecord(c->e1, st));
-    GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
+    // The path rebuild follows on the stream (it checks the status itself);
+    // the control block and the path's first words come back together.
+    unsigned long long* const used = reinterpret_cast<unsigned long long*>(lb + kLbUsed);
+    uint64_t prefix = 0;
+    if (want_path) {
+        const uint64_t arena_words =
+            pp.kind == KIND_GRID ? (uint64_t)pp.W * pp.H + 2 : kPathArenaWords;  // a grid path visits a cell once
+        if (!c->path.ensure(arena_words * 8 + 16)) return GASTAR_OUT_OF_MEMORY;
+        rc = launch_paths(P.insts, 1, reinterpret_cast<unsigned long long*>(c->path.p), c->path.n / 8, used, st);
+        if (rc != GASTAR_OK) return rc;
+        ++as.launches;
+        prefix = std::min<uint64_t>(kPathPrefixWords, c->path.n / 8);
+        GA_CUDA(cudaMemcpyAsync(c->h_path, c->path.p, prefix * 8, cudaMemcpyDeviceToHost, st));
+        as.d2h += prefix * 8;
+    }
+    GA_CUDA(cudaMemcpyAsync(c->h_ctl, lb + kLbCtl, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
     GA_CUDA(cudaStreamSynchronize(st));
     as.d2h += sizeof(InstCtl);
     if (pp.kind != KIND_GRID) {
@@ -510,19 +542,37 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         // list's size some claims went unrecorded.
         if (1 + c->h_ctl->table_used + heaps * kTouchedChunk > touched_cap) c->table_dirty = true;
     }
-    if (want_path && c->h_ctl->status == ST_OK) {
-        // best + 1 states is the longest possible path (every step costs >= 1).
+    if (want_path && c->h_ctl->status == ST_PATH_CAP && c->h_ctl->best != kInf) {
+        // Longer than the first arena: again with room for best + 1 states
+        // (every step costs >= 1).
         const uint64_t words = ((uint64_t)c->h_ctl->best + 2) * kw;
-        if (!c->path.ensure(words * 8 + 16) || !c->misc.ensure(64)) return GASTAR_OUT_OF_MEMORY;
-        unsigned long long* used = reinterpret_cast<unsigned long long*>(c->misc.p) + 2;
+        if (!c->path.ensure(words * 8 + 16)) return GASTAR_OUT_OF_MEMORY;
+        InstCtl* hc = reinterpret_cast<InstCtl*>(hl + kLbCtl);
+        *hc = *c->h_ctl;
+        hc->status = ST_OK;
+        hc->path_len = 0;
+        GA_CUDA(cudaMemcpyAsync(lb + kLbCtl, hc, sizeof(InstCtl), cudaMemcpyHostToDevice, st));
         GA_CUDA(cudaMemsetAsync(used, 0, 8, st));
-        rc = launch_paths(reinterpret_cast<const InstDesc*>(c->desc.p), 1,
-                          reinterpret_cast<unsigned long long*>(c->path.p), words, used, st);
+        rc = launch_paths(P.insts, 1, reinterpret_cast<unsigned long long*>(c->path.p), c->path.n / 8, used, st);
         if (rc != GASTAR_OK) return rc;
         ++as.launches;
-        GA_CUDA(cudaMemcpyAsync(c->h_ctl, c->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
+        prefix = 0;
+        GA_CUDA(cudaMemcpyAsync(c->h_ctl, lb + kLbCtl, sizeof(InstCtl), cudaMemcpyDeviceToHost, st));
         GA_CUDA(cudaStreamSynchronize(st));
+        as.h2d += sizeof(InstCtl);
         as.d2h += sizeof(InstCtl);
+    }
+    if (want_path && c->h_ctl->status == ST_OK) {
+        const uint64_t words = (uint64_t)c->h_ctl->path_len * kw, off = c->h_ctl->path_off;
+        path_keys->resize(words);
+        if (off + words <= prefix) {
+            std::memcpy(path_keys->data(), c->h_path + off, words * 8);
+        } else {
+            GA_CUDA(cudaMemcpyAsync(path_keys->data(), reinterpret_cast<unsigned long long*>(c->path.p) + off,
+                                    words * 8, cudaMemcpyDeviceToHost, st));
+            GA_CUDA(cudaStreamSynchronize(st));
+            as.d2h += words * 8;
+        }
     }
     float ms = 0;
     GA_CUDA(cudaEventElapsedTime(&ms, c->e0, c->e1));
@@ -550,7 +600,7 @@ int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user
     uint32_t attempts = 0;
     for (;;) {
         ++attempts;
-        int rc = plain_attempt(c, pp, cfg, table_log2, heap_entries, path_keys != nullptr, st, ctl, as);
+        int rc = plain_attempt(c, pp, cfg, table_log2, heap_entries, path_keys, st, ctl, as);
         if (rc != GASTAR_OK) return rc;
         if (!cfg.regrow) break;
         if (ctl.status == ST_TABLE_FULL && pp.kind != KIND_GRID && table_log2 < max_log2) {
@@ -570,15 +620,6 @@ int plain_solve(gastar_ctx* c, const PlainProblem& pp, const gastar_config* user
     out->h2d_bytes = as.h2d;
     out->d2h_bytes = as.d2h;
     c->launches += as.launches;
-    if (path_keys && ctl.status == ST_OK) {
-        const uint32_t kw = key_words(pp.kind);
-        path_keys->resize((size_t)ctl.path_len * kw);
-        GA_CUDA(cudaMemcpyAsync(path_keys->data(),
-                                reinterpret_cast<unsigned long long*>(c->path.p) + ctl.path_off,
-                                path_keys->size() * 8, cudaMemcpyDeviceToHost, st));
-        GA_CUDA(cudaStreamSynchronize(st));
-        out->d2h_bytes += path_keys->size() * 8;
-    }
     return GASTAR_OK;
 }
 

@@ -75,11 +75,14 @@ struct gastar_ctx {
     char name[256] = {0};
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    gastar::DevBuf table, dense, touched, heaps, hdr, stage, desc, ctl, team, path, misc, weights, buckets;
+    gastar::DevBuf table, dense, touched, heaps, hdr, stage, path, misc, weights, buckets;
+    // Plain engine: descriptor, control block, team control and counters of
+    // one solve in one device block, uploaded from a pinned mirror in one copy.
+    gastar::DevBuf launch;
+    void* h_launch = nullptr;      // pinned
+    uint64_t* h_path = nullptr;    // pinned: the path's first words, read back with the control block
     bool table_dirty = true;       // hash table needs a full clear before the next solve
     uint32_t prev_slot_words = 2;  // slot width of the solve that filled the touched list
     uint64_t launches = 0;         // kernels launched by this context
     gastar::InstCtl* h_ctl = nullptr;  // pinned
-    gastar::InstDesc h_desc;
-    gastar::TeamCtl h_team;
 };
