@@ -384,30 +384,37 @@ __device__ __forceinline__ uint32_t ld_vol(const uint32_t* p) { return *(const v
 __device__ __forceinline__ uint64_t ld_vol64(const unsigned long long* p) {
     return *(const volatile unsigned long long*)p;
 }
-__device__ __forceinline__ void st_vol(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
 
-// Waits (one thread) until *p >= target: bounded by the deadline, released
-// by the team's abort flag; a timeout raises the flag.  The fence after the
-// wait orders the reads that follow after the writes the waited-for block
-// made before raising *p.
-__device__ __forceinline__ bool team_wait_u32(const uint32_t* p, uint32_t target, TeamCtl* tc,
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add_u32(uint32_t* p, uint32_t v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits (one thread) until *p >= target, given `seen`, a value of *p read
+// with acquire before: bounded by the deadline, released by the team's abort
+// flag; a timeout raises the flag.  Returns with acquire ordering: the writes
+// the waited-for block made before raising *p are visible.
+__device__ __forceinline__ bool team_wait_u32(const uint32_t* p, uint32_t target, uint32_t seen, TeamCtl* tc,
                                               uint64_t timeout_ns) {
-    const volatile uint32_t* vp = p;
-    if (*vp < target) {
-        const volatile uint32_t* vab = &tc->abort;
-        const uint64_t t0 = globaltimer_ns();
-        for (uint32_t spin = 1;; ++spin) {
-            if (*vp >= target) break;
-            if (*vab) return false;
-            if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
-                atomicExch(&tc->abort, 1u);
-                return false;
-            }
-            if (spin > 64) __nanosleep(32);
+    if (seen >= target) return true;
+    const volatile uint32_t* vab = &tc->abort;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        if (ld_acquire_u32(p) >= target) return true;
+        if (*vab) return false;
+        if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+            atomicExch(&tc->abort, 1u);
+            return false;
         }
+        if (spin > 64) __nanosleep(32);
     }
-    asm volatile("fence.acq_rel.gpu;" ::: "memory");
-    return true;
 }
 
 // The blocks working on one instance.
@@ -624,6 +631,10 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                     if (d.max_iter && it0 + it + 1 >= d.max_iter) err = ST_BUDGET;
                     if (d.timeout_ns && globaltimer_ns() - sm.t_start > d.timeout_ns) err = ST_TIMEOUT;
                 }
+                // The cut to test is read first: its round trip overlaps this
+                // block's publication.
+                const CutSlot* t = cuts + (it + kCuts - kCutLag) % kCuts;
+                const uint32_t tseen = it >= kCutLag ? ld_acquire_u32(&t->count) : 0u;
                 CutSlot* c = cuts + it % kCuts;
                 if (sm.agg_minprio != kInfPrio) atomicMin(&c->minprio, sm.agg_minprio);
                 if (sm.cnt[4] != sm.pub[0]) atomicAdd(&c->claims, sm.cnt[4] - sm.pub[0]);
@@ -633,8 +644,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
                 if (lossy) atomicCAS(&c->lossy, 0u, lossy);
                 if (err) atomicCAS(&c->err, 0u, err);
-                asm volatile("fence.acq_rel.gpu;" ::: "memory");
-                atomicAdd(&c->count, 1u);
+                red_release_add_u32(&c->count, 1u);  // the updates above precede the arrival
                 sm.agg.best = kInf;
                 sm.agg.err = 0;
                 sm.agg.count = 0;
@@ -643,8 +653,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 uint32_t dec = kInf, dbest = kInf, dfmin = kInf;
                 if (it >= kCutLag) {
                     // Waits only while a block is more than kCutLag iterations behind.
-                    const CutSlot* t = cuts + (it - kCutLag) % kCuts;
-                    if (!team_wait_u32(&t->count, tm.ctas, tm.ctl, P.barrier_timeout_ns)) {
+                    if (!team_wait_u32(&t->count, tm.ctas, tseen, tm.ctl, P.barrier_timeout_ns)) {
                         dec = ST_BARRIER;
                     } else {
                         const uint64_t open_min = ld_vol64(&t->minprio);
@@ -874,14 +883,20 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             __syncthreads();  // every warp's stage writes are done
             if (threadIdx.x == 0) {
                 const uint32_t row = (it % kStageRing) * tm.ctas;
+                const uint32_t from = (rank + it) % tm.ctas;
+                // The producer's flag is read first: its round trip overlaps
+                // this block's own publication.
+                const uint32_t seen = ld_acquire_u32(ready + from);
                 __stcg(ring_counts + row + rank, sm.agg.count);
                 sm.agg.count = 0;
-                asm volatile("fence.acq_rel.gpu;" ::: "memory");
-                st_vol(ready + rank, it + 1);
-                const uint32_t from = (rank + it) % tm.ctas;
+                // Release: every warp's stage writes (ordered before thread 0
+                // by the block barrier) and the count precede the flag.
+                st_release_u32(ready + rank, it + 1);
                 uint32_t dec = kInf, n = 0;
-                if (!team_wait_u32(ready + from, it + 1, tm.ctl, P.barrier_timeout_ns)) dec = ST_BARRIER;
-                else n = __ldcg(ring_counts + row + from);
+                if (!team_wait_u32(ready + from, it + 1, from == rank ? it + 1 : seen, tm.ctl, P.barrier_timeout_ns))
+                    dec = ST_BARRIER;
+                else
+                    n = __ldcg(ring_counts + row + from);
                 sm.dec_status = dec;
                 sm.push_count = n;
             }
