@@ -167,3 +167,15 @@ def test_grid_edge_cases(engine, oracle, gastar):
         assert r.status_name == "OK" and ok and cost == r.cost
         if heur == gastar.H_ZERO:
             assert r.cost == o.cost
+
+
+@pytest.mark.parametrize("delta", [36, 0])
+def test_4096_grid_full_size(engine, oracle, gastar, delta):
+    """The plain grid configuration at full size: 4096 x 4096, weights 1..9,
+    20 % obstacles, a monotone corridor from (0, 0) to (4095, 4095); optimal
+    cost equal to the oracle's and a valid path (with and without the pop
+    window)."""
+    wts = gastar.gen_grid(4096, 4096, 0x4096, 0.2)
+    r = engine.solve_grid(wts, (0, 0), (4095, 4095), num_queues=16384, delta=delta)
+    _check_grid(oracle, wts, (0, 0), (4095, 4095), r)
+    assert len(r.path) > 4095 and r.path[0] == 0 and r.path[-1] == 4096 * 4096 - 1
