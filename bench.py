@@ -152,6 +152,28 @@ def _mixed_instances(g):
     return p15, grids
 
 
+def run_grid4k(g, eng, check: bool) -> dict:
+    """Plain GA* on the 4096 x 4096 weighted grid (weights 1..9, 20 %
+    obstacles, monotone corridor (0,0) -> (4095,4095)): device time of the
+    solve, expansions/s, and its cost against the CPU oracle."""
+    wts = g.gen_grid(4096, 4096, 0x4096, 0.2)
+    cfg = g.make_config(num_queues=16384, delta=36)
+    eng.solve_grid(wts, (0, 0), (4095, 4095), config=cfg)  # warm-up
+    runs = [eng.solve_grid(wts, (0, 0), (4095, 4095), config=cfg) for _ in range(3)]
+    r = min(runs, key=lambda x: x.kernel_ms)
+    out = {"workload": "plain GA*, 4096x4096 grid, weights 1-9, 20% obstacles, corridor; Q=16384, "
+                       "pop window 36",
+           "kernel_ms": r.kernel_ms, "total_ms": r.total_ms, "cost": r.cost,
+           "node_expansions_per_s": r.expansions / (r.kernel_ms / 1000.0)}
+    if check:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib as o
+        ref, _ = o.grid_astar(wts, (0, 0), (4095, 4095), path=False)
+        out["oracle_cost"] = ref.cost
+        out["optimal_cost_agreement"] = float(ref.cost == r.cost)
+    return out
+
+
 def run_batched(g, eng, steps: int) -> dict:
     """Batched mixed workload: one persistent launch over 1024 instances (autotuned),
     against the plain engine on a stratified 64-instance sample of the mix."""
@@ -461,6 +483,8 @@ def run_ours(args) -> dict:
                                "sample": f"the same {n_inst} instances once, single-thread host "
                                          f"A* per instance over {used} threads"}
         out["optimal_cost_agreement"] = agree
+    if rank == 0 and world == 1:
+        out["grid_4096"] = run_grid4k(g, eng, check=not args.no_cpu_baseline)
     if rank == 0 and world == 1 and not args.no_batched:
         out["batched"] = run_batched(g, eng, max(1, min(args.steps, 3)))
         ra = out["roofline"].get("random_access", {})
