@@ -1,21 +1,26 @@
 // The GA* search: problem domains and the persistent search kernel.
 //
 // One "team" of thread blocks works on one instance; each warp of the team
-// owns one warp-heap.  An iteration is
+// owns one open list (a warp-heap, optionally behind a bucket front).  An
+// iteration is
 //   pop    : every warp pops up to `ew` best entries (one per lane), drops
 //            stale ones (table g lower than the entry's g) and goal states;
 //   expand : every lane generates the successors of its entry, computes g and
 //            an incrementally updated h, and does one insert-or-min on the
 //            duplicate-detection table per successor; improved successors go
-//            to the team's stage buffer (shared memory for one-block teams);
-//   push   : after a team barrier, stage chunks are dealt round-robin (with a
-//            rotating offset) to the warp-heaps, which push them;
-//   check  : the team's minimum priority is reduced; the search ends when the
-//            best goal cost is <= min f over all open entries.
+//            to the block's stage area;
+//   push   : one-block teams deal their stage chunks round-robin (rotating
+//            offset) to their warps after a block barrier; in a multi-block
+//            team block c pushes the stage region of block (c + i) mod blocks
+//            once that block has flagged it ready (no team barrier);
+//   check  : the search ends when the best goal cost is <= min f over all
+//            open entries -- over the block's slots (one-block teams) or over
+//            the cut every block publishes per iteration (multi-block teams,
+//            tested kCutLag iterations later).
 // This is the reference's iteration (a_star.h:247-264: extract_nodes, three
 // bitonic sorts, mark_duplicates, insert_unique_data, remove_updated_elements,
 // insert_nodes_into_queues, two host reductions) as one device-resident loop
-// with two barriers and no host round trip.
+// with no host round trip.
 #pragma once
 
 #include <type_traits>
@@ -685,9 +690,9 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             }
             if (status != kInf) break;
         } else if (leader) {
-            // Slot it+1 was last read right after the barrier of iteration
-            // it-2; every block is past that point, and none writes it before
-            // the barrier of this iteration.
+            // One-block team: slot it+1 was last read right after the block
+            // barrier of iteration it-2; every warp is past that point, and
+            // none writes it before the barrier of this iteration.
             TeamSlot* nx = slots + (it + 1) % kSlots;
             nx->minprio = kInfPrio;
             nx->minstage = kInfPrio;
