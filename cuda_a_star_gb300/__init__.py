@@ -261,6 +261,18 @@ class Batch:
             p = buf
         return SolveResult.from_c(r, p)
 
+    def timeline(self):
+        """(start_ns, end_ns) arrays of the last run's persistent launch, one
+        entry per instance, from the earliest start; 0, 0 where none ran."""
+        import numpy as np
+        n = len(self)
+        s = np.zeros(n, dtype=np.uint64)
+        e = np.zeros(n, dtype=np.uint64)
+        _check(lib().gastar_batch_timeline(self._h, s.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                           e.ctypes.data_as(C.POINTER(C.c_uint64))),
+               "gastar_batch_timeline")
+        return s, e
+
     def stats(self) -> dict:
         ms, h2d, d2h, dev = C.c_float(), C.c_uint64(), C.c_uint64(), C.c_uint64()
         lib().gastar_batch_stats(self._h, C.byref(ms), C.byref(h2d), C.byref(d2h), C.byref(dev))

@@ -21,7 +21,7 @@ EXPORTS = [
     "gastar_batch_config_default", "gastar_batch_create", "gastar_batch_destroy",
     "gastar_batch_add_sliding", "gastar_batch_add_grid", "gastar_batch_run",
     "gastar_batch_rerun", "gastar_batch_count", "gastar_batch_result", "gastar_batch_path",
-    "gastar_batch_stats", "gastar_batch_autotune", "gastar_batch_phases",
+    "gastar_batch_stats", "gastar_batch_autotune", "gastar_batch_phases", "gastar_batch_timeline",
     "gastar_serve_config_default", "gastar_serve_create", "gastar_serve_destroy",
     "gastar_serve_submit_sliding", "gastar_serve_submit_grid", "gastar_serve_step",
     "gastar_serve_poll", "gastar_serve_release", "gastar_serve_stats",
@@ -125,6 +125,7 @@ def load(path: str | None = None) -> C.CDLL:
                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "gastar_batch_phases": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.POINTER(C.c_float), u32p, u32p]),
+        "gastar_batch_timeline": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "gastar_batch_autotune": (C.c_int, [vp, C.c_uint32, C.c_char_p, C.POINTER(BatchConfig),
                                             C.POINTER(C.c_float)]),
         "gastar_serve_config_default": (None, [C.POINTER(ServeConfig)]),

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -73,9 +74,12 @@ struct gastar_batch {
     uint32_t retry_level = 0;   // partitions scale by 4^retry_level
     uint32_t retried = 0;       // instances re-solved with larger partitions in the last run
     double block_share = 0;     // > 0: use this share of the resident blocks (autotuner trials)
+    gastar_batch* sub = nullptr;    // re-run batch of the last run's overflowed instances,
+    std::vector<uint32_t> sub_idx;  // kept while the same instances overflow
     bool uploaded = false;
     DevBuf arena, weights, descs, ctls, order, counters, paths;
     std::vector<InstDesc> h_desc;
+    std::vector<uint64_t> tl_start, tl_end;  // the persistent launch's schedule (globaltimer ns)
     InstCtl* h_ctl = nullptr;               // pinned, n + 1 (last = arena counter)
     std::vector<unsigned long long> h_paths;
     uint64_t path_words = 0;
@@ -128,6 +132,7 @@ void gastar_batch_destroy(gastar_batch* b) {
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    gastar_batch_destroy(b->sub);
     b->arena.release();
     b->weights.release();
     b->descs.release();
@@ -221,15 +226,16 @@ int batch_upload(gastar_batch* b) {
     b->heavy.assign(n, 0);
     b->promotable.assign(n, 0);
     b->n_heavy = 0;
-    uint64_t heavy_est = 0, total_est = 0;
+    uint64_t heavy_est = 0, total_est = 0, heavy_min = ~0ull;
     for (uint32_t i = 0; i < n; ++i) {
         const Problem& p = b->insts[i];
-        const uint64_t work = p.kind == KIND_GRID ? (uint64_t)p.W * p.H : (1ull << 16);
+        const uint64_t work = p.est;
         total_est += work;
         if (T > 1 && p.kind == KIND_GRID && (uint64_t)p.W * p.H >= b->cfg.heavy_cells) {
             b->heavy[i] = 1;
             ++b->n_heavy;
             heavy_est += work;
+            heavy_min = std::min(heavy_min, work);
         }
         const uint64_t pe = b->cfg.promote_expansions;
         if (p.kind != KIND_GRID && p.n >= 4 && pe && (!b->cfg.max_expansions || b->cfg.max_expansions > pe))
@@ -237,8 +243,17 @@ int batch_upload(gastar_batch* b) {
     }
     b->heavy_teams = 0;
     if (b->n_heavy) {
-        const double share = total_est ? (double)heavy_est / (double)total_est : 1.0;
-        b->heavy_teams = (uint32_t)std::max<double>(1.0, share * b->blocks / T + 0.5);
+        // Enough teams that the heavy queue, whose instances each hold a team
+        // for est / T, ends no later than the one-block queue: the heavy work
+        // over the expected makespan less the time of the last (smallest)
+        // heavy instance, which a team takes when the others are nearly done.
+        // Teams that run out of heavy instances take one-block instances, so a
+        // team too many costs little; a team too few leaves the heavy
+        // instances as the tail.
+        const double M = (double)total_est / b->blocks;
+        const double tail = (double)heavy_min / T;
+        const double need = (double)heavy_est / std::max(M - tail, 0.5 * M);
+        b->heavy_teams = (uint32_t)std::max<double>(1.0, std::ceil(need / T));
         b->heavy_teams = std::min(b->heavy_teams, b->n_heavy);
         b->heavy_teams = std::min(b->heavy_teams, b->blocks / T);
         if (b->heavy_teams == 0) {  // too few blocks for a team: no teams
@@ -294,7 +309,7 @@ int batch_upload(gastar_batch* b) {
         if (b->insts[i].unreachable) continue;
         (b->heavy[i] ? horder : order).push_back(i);
     }
-    auto by_est = [&](uint32_t a, uint32_t bb) { return b->insts[a].est > b->insts[bb].est; };
+    auto by_est = [&](uint32_t a, uint32_t bb) { return sched_before(b->insts[a], b->insts[bb]); };
     std::stable_sort(order.begin(), order.end(), by_est);
     std::stable_sort(horder.begin(), horder.end(), by_est);
     b->n_sched = (uint32_t)order.size();
@@ -394,6 +409,12 @@ int batch_finish(gastar_batch* b) {
             return GASTAR_CUDA_ERROR;
         b->d2h += words * 8;
     }
+    b->tl_start.resize(n);
+    b->tl_end.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        b->tl_start[i] = b->h_ctl[i].t_start;
+        b->tl_end[i] = b->h_ctl[i].t_end;
+    }
     // Instances the standard move set cannot solve never ran a search.
     for (uint32_t i = 0; i < n; ++i)
         if (b->insts[i].unreachable) {
@@ -423,7 +444,9 @@ namespace {
 // Re-solves the instances whose partition overflowed (or whose path did not
 // fit the arena) in a follow-up batch with 4x larger partitions, then merges
 // their control blocks and paths back.  The follow-up batch retries its own
-// overflows the same way, down to 64x the class size.
+// overflows the same way, down to 64x the class size, and is kept for the
+// next run while the same instances overflow (a rerun replays it without new
+// allocations or uploads).
 // Few overflowed instances are left to the plain engine (re-solved one at a
 // time on the whole GPU with a growing table, see batch_promote): a second
 // batch launch over a handful of instances would keep most SMs idle.
@@ -439,11 +462,18 @@ int batch_retry_overflows(gastar_batch* b) {
     for (uint32_t i = 0; i < n; ++i)
         if (overflowed(b->h_ctl[i].status)) bad.push_back(i);
     if (bad.size() <= kPlainOverflowMax) return GASTAR_OK;
-    gastar_batch* sub = gastar_batch_create(b->ctx, &b->cfg);
-    if (!sub) return GASTAR_OUT_OF_MEMORY;
-    sub->cfg.use_graph = 0;
-    sub->retry_level = b->retry_level + 1;
-    for (uint32_t i : bad) sub->insts.push_back(b->insts[i]);
+    const bool fresh = !b->sub || b->sub_idx != bad;
+    if (fresh) {
+        gastar_batch_destroy(b->sub);
+        b->sub = gastar_batch_create(b->ctx, &b->cfg);
+        b->sub_idx.clear();
+        if (!b->sub) return GASTAR_OUT_OF_MEMORY;
+        b->sub->cfg.use_graph = 0;
+        b->sub->retry_level = b->retry_level + 1;
+        for (uint32_t i : bad) b->sub->insts.push_back(b->insts[i]);
+        b->sub_idx = bad;
+    }
+    gastar_batch* sub = b->sub;
     int rc = gastar_batch_run(sub);
     if (rc == GASTAR_OK) {
         b->retried = (uint32_t)bad.size();
@@ -462,10 +492,13 @@ int batch_retry_overflows(gastar_batch* b) {
         }
         b->kernel_ms += sub->kernel_ms;
         b->retry_ms += sub->kernel_ms;
-        b->h2d += sub->h2d;
+        if (fresh) b->h2d += sub->h2d;  // a kept re-run batch uploads nothing again
         b->d2h += sub->d2h;
+    } else {
+        gastar_batch_destroy(b->sub);
+        b->sub = nullptr;
+        b->sub_idx.clear();
     }
-    gastar_batch_destroy(sub);
     return rc;
 }
 
@@ -623,12 +656,29 @@ int gastar_batch_phases(gastar_batch* b, float* main_ms, float* retry_ms, float*
     return GASTAR_OK;
 }
 
+int gastar_batch_timeline(gastar_batch* b, uint64_t* start_ns, uint64_t* end_ns) {
+    if (!b || !start_ns || !end_ns || b->tl_start.size() != b->insts.size()) return GASTAR_BAD_INPUT;
+    const size_t n = b->tl_start.size();
+    uint64_t t0 = ~0ull;
+    for (size_t i = 0; i < n; ++i)
+        if (b->tl_start[i] && b->tl_end[i] >= b->tl_start[i]) t0 = std::min(t0, b->tl_start[i]);
+    for (size_t i = 0; i < n; ++i) {
+        const bool ran = b->tl_start[i] && b->tl_end[i] >= b->tl_start[i];
+        start_ns[i] = ran ? b->tl_start[i] - t0 : 0;
+        end_ns[i] = ran ? b->tl_end[i] - t0 : 0;
+    }
+    return GASTAR_OK;
+}
+
 int gastar_batch_stats(gastar_batch* b, float* kernel_ms, uint64_t* h2d, uint64_t* d2h, uint64_t* dev) {
     if (!b) return GASTAR_BAD_INPUT;
     if (kernel_ms) *kernel_ms = b->kernel_ms;
     if (h2d) *h2d = b->h2d;
     if (d2h) *d2h = b->d2h;
-    if (dev) *dev = b->device_bytes;
+    if (dev) {  // with the kept re-run batches
+        *dev = 0;
+        for (const gastar_batch* x = b; x; x = x->sub) *dev += x->device_bytes;
+    }
     return GASTAR_OK;
 }
 

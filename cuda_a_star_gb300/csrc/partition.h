@@ -16,8 +16,20 @@ struct Problem {
     uint32_t W = 0, H = 0, minw = 0, f0 = 0;
     bool unreachable = false;      // other parity class of the standard sliding moves
     std::vector<uint8_t> weights;  // grid
-    uint64_t est = 0;              // scheduling estimate (larger first)
+    uint64_t est = 0;              // expected one-block search time in ns
 };
+
+// Launch order inside a persistent launch (longest processing time first):
+// 15- and 24-puzzles first -- their time is not predictable from the start
+// state, but their partition bounds it (about 100 ms on one block before it
+// fills), so the long ones among them start early instead of forming the
+// tail -- then by expected time, largest first, so that the small grids fill
+// the end.
+inline bool sched_before(const Problem& a, const Problem& b) {
+    const bool ua = a.kind != KIND_GRID && a.n >= 4, ub = b.kind != KIND_GRID && b.n >= 4;
+    if (ua != ub) return ua;
+    return a.est > b.est;
+}
 
 // Sizing knobs of a partition.
 struct PartConfig {

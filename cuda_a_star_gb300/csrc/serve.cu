@@ -339,10 +339,10 @@ int gastar_serve_step(gastar_server* s) {
             (s->reqs[s->slot_req[i]].heavy ? heavy : light).push_back(i);
         }
     if (active.empty()) return GASTAR_OK;
-    // Larger remaining work first inside the launch; the order array holds the
-    // one-block requests, then the heavy ones.
+    // Longest work first inside the launch (sched_before); the order array
+    // holds the one-block requests, then the heavy ones.
     auto by_est = [&](uint32_t a, uint32_t b) {
-        return s->reqs[s->slot_req[a]].prob.est > s->reqs[s->slot_req[b]].prob.est;
+        return sched_before(s->reqs[s->slot_req[a]].prob, s->reqs[s->slot_req[b]].prob);
     };
     std::stable_sort(light.begin(), light.end(), by_est);
     std::stable_sort(heavy.begin(), heavy.end(), by_est);

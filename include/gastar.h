@@ -201,6 +201,11 @@ int gastar_batch_stats(gastar_batch *b, float *kernel_ms, uint64_t *h2d_bytes,
  * of promoted puzzles; with how many instances took the last two. */
 int gastar_batch_phases(gastar_batch *b, float *main_ms, float *retry_ms, float *promote_ms,
                         uint32_t *retried, uint32_t *promoted);
+/* Schedule of the last run's persistent launch: per instance (count entries),
+ * the device times at which its search started and ended, in ns from the
+ * earliest start; 0 and 0 for an instance that did not run (unreachable).
+ * Re-runs and re-solves after the launch are not included. */
+int gastar_batch_timeline(gastar_batch *b, uint64_t *start_ns, uint64_t *end_ns);
 
 /* ---- served GA*: continuous batching of solve requests ----
  * No reference counterpart (one instance per process there).  Requests wait in

@@ -46,6 +46,14 @@ def test_mixed_batch_matches_oracle(engine, oracle, gastar, open_list):
     assert [b.result(i, path=False).cost for _, _, _, i in cases] == costs
     st = b.stats()
     assert st["kernel_ms"] > 0 and st["device_bytes"] > 0
+    # The launch's schedule: every solved instance ran inside the launch,
+    # the unreachable board never started.
+    t0, t1 = b.timeline()
+    bad_idx = cases[-1][3]
+    assert t0[bad_idx] == 0 and t1[bad_idx] == 0
+    ran = [i for _, _, _, i in cases if i != bad_idx]
+    assert all(t1[i] >= t0[i] for i in ran) and min(t0[i] for i in ran) == 0
+    assert max(t1[i] for i in ran) <= (st["main_ms"] + 1.0) * 1e6
     b.close()
 
 
@@ -75,6 +83,13 @@ def test_batch_partition_overflow_is_retried(engine, oracle, gastar, count):
         assert st["retried"] == 0 and st["promoted"] > 0
     else:
         assert st["retried"] > 64
+    for i, (s, g) in enumerate(inst):
+        r = b.result(i)
+        o, _ = oracle.sliding_astar(4, s, g, path=False)
+        assert r.status_name == "OK" and r.cost == o.cost
+        assert oracle.sliding_validate(4, s, g, r.path) == (True, r.cost)
+    b.rerun()  # the kept re-run batch is replayed
+    assert b.stats()["retried"] == st["retried"]
     for i, (s, g) in enumerate(inst):
         r = b.result(i)
         o, _ = oracle.sliding_astar(4, s, g, path=False)
