@@ -27,12 +27,13 @@ inline __host__ __device__ size_t stage_entries_per_buffer(uint32_t heaps, uint3
 
 // Multi-block teams run their iterations without a team barrier.  Block b
 // stages its successors of iteration i into region b of stage buffer
-// i % kStageRing and then raises ready[b] to i + 1; block c pushes the region
-// of block (c + i) % blocks once that block is ready.  The termination test of
-// the cut at the start of iteration i (every block's heap minimum, goals and
-// errors) is evaluated at iteration i + kCutLag, so no block runs more than
-// kCutLag iterations ahead of another, and a stage buffer is always consumed
-// before it is written again.
+// i % kStageRing; after its expansion it publishes, behind one release fence,
+// ready[b] = i + 1 and its part of cut i (heap minimum after the previous
+// push, minimum of what it staged, goals, errors, counts).  Block c then
+// pushes the region of block (c + i) % blocks once that block is ready.  Cut
+// i is tested at iteration i + kCutLag, so no block runs more than kCutLag
+// iterations ahead of another, and a stage buffer is always consumed before
+// it is written again.
 constexpr uint32_t kStageRing = 4;
 constexpr uint32_t kCutLag = 2;
 constexpr uint32_t kCuts = 16;  // cut slots in the ring (> 3 * kCutLag + 2)

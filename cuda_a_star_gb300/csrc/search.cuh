@@ -15,8 +15,9 @@
 //            once that block has flagged it ready (no team barrier);
 //   check  : the search ends when the best goal cost is <= min f over all
 //            open entries -- over the block's slots (one-block teams) or over
-//            the cut every block publishes per iteration (multi-block teams,
-//            tested kCutLag iterations later).
+//            the cut every block publishes with its stage region, one
+//            hand-off per iteration (multi-block teams, tested kCutLag
+//            iterations later).
 // This is the reference's iteration (a_star.h:247-264: extract_nodes, three
 // bitonic sorts, mark_duplicates, insert_unique_data, remove_updated_elements,
 // insert_nodes_into_queues, two host reductions) as one device-resident loop
@@ -395,11 +396,13 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+// Strong relaxed writes: after fence_acq_rel_gpu they form release patterns.
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void red_release_add_u32(uint32_t* p, uint32_t v) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void red_relaxed_add_u32(uint32_t* p, uint32_t v) {
+    asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Waits (one thread) until *p >= target, given `seen`, a value of *p read
@@ -619,77 +622,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         TeamSlot* Sw = multi ? &sm.agg : S;
         E* const stage = multi ? stage0 + ((size_t)(it % kStageRing) * tm.ctas + rank) * region_cap
                                : stage0 + (size_t)(it & 1) * stage_cap;
-        if (multi) {
-            // ---- publish cut `it`, test cut it - kCutLag (a_star.h:260-262) ----
-            __syncthreads();  // the previous push is complete in every warp
-            if (threadIdx.x == 0) {
-                CutSlot* cuts = tm.ctl->cut;
-                uint32_t lossy = sm.agg.err ? sm.agg.err : sm.agg_err_prev, err = 0;
-                if (leader) {
-                    if (it >= 2 * kCutLag + 2) {  // every block has read it; none writes it yet
-                        CutSlot* r = cuts + (it - 2 * kCutLag - 2) % kCuts;
-                        r->minprio = kInfPrio;
-                        r->claims = r->exps = 0;
-                        r->best = kInf;
-                        r->lossy = r->err = r->count = 0;
-                    }
-                    if (d.max_iter && it0 + it + 1 >= d.max_iter) err = ST_BUDGET;
-                    if (d.timeout_ns && globaltimer_ns() - sm.t_start > d.timeout_ns) err = ST_TIMEOUT;
-                }
-                // The cut to test is read first: its round trip overlaps this
-                // block's publication.
-                const CutSlot* t = cuts + (it + kCuts - kCutLag) % kCuts;
-                const uint32_t tseen = it >= kCutLag ? ld_acquire_u32(&t->count) : 0u;
-                CutSlot* c = cuts + it % kCuts;
-                if (sm.agg_minprio != kInfPrio) atomicMin(&c->minprio, sm.agg_minprio);
-                if (sm.cnt[4] != sm.pub[0]) atomicAdd(&c->claims, sm.cnt[4] - sm.pub[0]);
-                if (sm.cnt[0] != sm.pub[1]) atomicAdd(&c->exps, sm.cnt[0] - sm.pub[1]);
-                sm.pub[0] = sm.cnt[4];
-                sm.pub[1] = sm.cnt[0];
-                if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
-                if (lossy) atomicCAS(&c->lossy, 0u, lossy);
-                if (err) atomicCAS(&c->err, 0u, err);
-                red_release_add_u32(&c->count, 1u);  // the updates above precede the arrival
-                sm.agg.best = kInf;
-                sm.agg.err = 0;
-                sm.agg.count = 0;
-                sm.agg_minprio = kInfPrio;
-                sm.agg_err_prev = 0;
-                uint32_t dec = kInf, dbest = kInf, dfmin = kInf;
-                if (it >= kCutLag) {
-                    // Waits only while a block is more than kCutLag iterations behind.
-                    if (!team_wait_u32(&t->count, tm.ctas, tseen, tm.ctl, P.barrier_timeout_ns)) {
-                        dec = ST_BARRIER;
-                    } else {
-                        const uint64_t open_min = ld_vol64(&t->minprio);
-                        dbest = ld_vol(&t->best);
-                        uint32_t tl = ld_vol(&t->lossy), te = ld_vol(&t->err);
-                        // Budgets from the team's totals, the same in every block.
-                        sm.run[0] += ld_vol64(&t->claims);
-                        sm.run[1] += ld_vol64(&t->exps);
-                        if (!tl && sm.base[0] + sm.run[0] > d.table_limit) tl = ST_TABLE_FULL;
-                        if (!te && d.max_exp && sm.base[1] + sm.run[1] >= d.max_exp) te = ST_BUDGET;
-                        const uint32_t bb = dbest < best_r ? dbest : best_r;
-                        if (tl) dec = tl;  // an iteration that lost entries proves nothing
-                        else if (bb != kInf && bb <= prio_f(open_min)) dec = ST_OK;
-                        else if (te) dec = te;
-                        else if (open_min == kInfPrio) dec = ST_NO_PATH;
-                        if (open_min != kInfPrio) dfmin = prio_f(open_min);
-                    }
-                }
-                sm.dec_status = dec;
-                sm.dec_best = dbest;
-                sm.dec_fmin = dfmin;
-            }
-            __syncthreads();
-            {
-                const uint32_t db = sm.dec_best;
-                best_r = db < best_r ? db : best_r;
-                if (sm.dec_fmin != kInf) fmin = sm.dec_fmin;
-                status = sm.dec_status;
-            }
-            if (status != kInf) break;
-        } else if (leader) {
+        if (!multi && leader) {
             // One-block team: slot it+1 was last read right after the block
             // barrier of iteration it-2; every warp is past that point, and
             // none writes it before the barrier of this iteration.
@@ -883,33 +816,99 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             }
         }
         if (multi) {
-            // Publish this block's region, then wait for the block whose
-            // region this block pushes.
-            __syncthreads();  // every warp's stage writes are done
+            // ---- one hand-off per iteration: publish cut `it` and this
+            // block's stage region, then wait for the region this block
+            // pushes and test cut it - kCutLag (a_star.h:260-262) ----
+            __syncthreads();  // every warp's stage writes and counters are done
             if (threadIdx.x == 0) {
+                CutSlot* cuts = tm.ctl->cut;
                 const uint32_t row = (it % kStageRing) * tm.ctas;
                 const uint32_t from = (rank + it) % tm.ctas;
-                // The producer's flag is read first: its round trip overlaps
-                // this block's own publication.
+                // Both awaited words are read first: their round trips overlap
+                // this block's publication.
                 const uint32_t seen = ld_acquire_u32(ready + from);
+                const CutSlot* t = cuts + (it + kCuts - kCutLag) % kCuts;
+                const uint32_t tseen = it >= kCutLag ? ld_acquire_u32(&t->count) : 0u;
+                const uint32_t lossy = sm.agg.err ? sm.agg.err : sm.agg_err_prev;
+                uint32_t err = 0;
+                if (leader) {
+                    if (it >= 2 * kCutLag + 2) {  // every block has read it; none writes it yet
+                        CutSlot* r = cuts + (it - 2 * kCutLag - 2) % kCuts;
+                        r->minprio = kInfPrio;
+                        r->claims = r->exps = 0;
+                        r->best = kInf;
+                        r->lossy = r->err = r->count = 0;
+                    }
+                    if (d.max_iter && it0 + it + 1 >= d.max_iter) err = ST_BUDGET;
+                    if (d.timeout_ns && globaltimer_ns() - sm.t_start > d.timeout_ns) err = ST_TIMEOUT;
+                }
+                // Cut `it` covers this block's heaps after the previous push
+                // (a superset of what is left after this iteration's pops) and
+                // what this iteration staged.
+                CutSlot* c = cuts + it % kCuts;
+                const unsigned long long cm =
+                    sm.agg_minprio < sm.agg.minstage ? sm.agg_minprio : sm.agg.minstage;
+                if (cm != kInfPrio) atomicMin(&c->minprio, cm);
+                if (sm.cnt[4] != sm.pub[0]) atomicAdd(&c->claims, sm.cnt[4] - sm.pub[0]);
+                if (sm.cnt[0] != sm.pub[1]) atomicAdd(&c->exps, sm.cnt[0] - sm.pub[1]);
+                sm.pub[0] = sm.cnt[4];
+                sm.pub[1] = sm.cnt[0];
+                if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
+                if (lossy) atomicCAS(&c->lossy, 0u, lossy);
+                if (err) atomicCAS(&c->err, 0u, err);
                 __stcg(ring_counts + row + rank, sm.agg.count);
+                // One release fence for both arrivals: every warp's stage
+                // writes (ordered before thread 0 by the block barrier), the
+                // region count and the cut's updates precede the ready flag
+                // and the cut arrival.
+                fence_acq_rel_gpu();
+                st_relaxed_u32(ready + rank, it + 1);
+                red_relaxed_add_u32(&c->count, 1u);
+                sm.agg.best = kInf;
+                sm.agg.err = 0;
                 sm.agg.count = 0;
-                // Release: every warp's stage writes (ordered before thread 0
-                // by the block barrier) and the count precede the flag.
-                st_release_u32(ready + rank, it + 1);
-                uint32_t dec = kInf, n = 0;
+                sm.agg.minstage = kInfPrio;
+                sm.agg_minprio = kInfPrio;
+                sm.agg_err_prev = 0;
+                uint32_t dec = kInf, n = 0, dbest = kInf, dfmin = kInf;
                 if (!team_wait_u32(ready + from, it + 1, from == rank ? it + 1 : seen, tm.ctl, P.barrier_timeout_ns))
                     dec = ST_BARRIER;
                 else
                     n = __ldcg(ring_counts + row + from);
+                if (dec == kInf && it >= kCutLag) {
+                    // Waits only while a block is more than kCutLag iterations behind.
+                    if (!team_wait_u32(&t->count, tm.ctas, tseen, tm.ctl, P.barrier_timeout_ns)) {
+                        dec = ST_BARRIER;
+                    } else {
+                        const uint64_t open_min = ld_vol64(&t->minprio);
+                        dbest = ld_vol(&t->best);
+                        uint32_t tl = ld_vol(&t->lossy), te = ld_vol(&t->err);
+                        // Budgets from the team's totals, the same in every block.
+                        sm.run[0] += ld_vol64(&t->claims);
+                        sm.run[1] += ld_vol64(&t->exps);
+                        if (!tl && sm.base[0] + sm.run[0] > d.table_limit) tl = ST_TABLE_FULL;
+                        if (!te && d.max_exp && sm.base[1] + sm.run[1] >= d.max_exp) te = ST_BUDGET;
+                        const uint32_t bb = dbest < best_r ? dbest : best_r;
+                        if (tl) dec = tl;  // an iteration that lost entries proves nothing
+                        else if (bb != kInf && bb <= prio_f(open_min)) dec = ST_OK;
+                        else if (te) dec = te;
+                        else if (open_min == kInfPrio) dec = ST_NO_PATH;
+                        if (open_min != kInfPrio) dfmin = prio_f(open_min);
+                    }
+                }
                 sm.dec_status = dec;
+                sm.dec_best = dbest;
+                sm.dec_fmin = dfmin;
                 sm.push_count = n;
             }
             __syncthreads();
-            if (sm.dec_status != kInf) {
+            {
+                const uint32_t db = sm.dec_best;
+                best_r = db < best_r ? db : best_r;
+                if (sm.dec_fmin != kInf) fmin = sm.dec_fmin;
                 status = sm.dec_status;
-                break;
             }
+            if (status != kInf) break;
         } else {
             if (!tsync()) {
                 status = ST_BARRIER;
