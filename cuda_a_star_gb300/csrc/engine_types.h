@@ -39,9 +39,6 @@ constexpr uint32_t kCutLag = 2;
 constexpr uint32_t kCuts = 16;  // cut slots in the ring (> 3 * kCutLag + 2)
 static_assert(kStageRing > kCutLag, "a stage buffer must be consumed before it is reused");
 
-// Global stage area of a multi-block team: kStageRing buffers, each one
-// region of warps*ew*maxn entries per block; then the entry count of every
-// region (kStageRing rows of `blocks` words) and the blocks' ready words.
 constexpr uint32_t kSlotsHost = 4;
 
 // Claim list: each warp reserves this many entries at a time; entries a warp
@@ -52,10 +49,14 @@ constexpr uint32_t kTouchedHole = 0xffffffffu;
 // Warp-heap nodes below sn live in shared memory (node 0 in registers).
 constexpr uint32_t kHeapSmemNodes = 7;      // default sn: nodes 1..6
 constexpr uint32_t kHeapSmemNodesMax = 127;  // levels 0..6
+// Global stage area of a multi-block team: kStageRing buffers, each one
+// region of warps*ew*maxn entries per block; then one 64-bit ready word per
+// region (kStageRing rows of `blocks` words): (iteration + 1) << 32 | the
+// region's entry count, written when the region is complete.
 inline __host__ __device__ size_t team_stage_bytes(uint32_t blocks, uint32_t warps, uint32_t ew, uint32_t maxn,
                                                    uint32_t entry_bytes) {
     const size_t entries = kStageRing * stage_entries_per_buffer(blocks * warps, ew, maxn);
-    return ((entries * entry_bytes + (size_t)(kStageRing + 1) * blocks * 4) + 15) & ~(size_t)15;
+    return ((entries * entry_bytes + (size_t)kStageRing * blocks * 8) + 15) & ~(size_t)15;
 }
 
 // Per-instance control block, written by the device.

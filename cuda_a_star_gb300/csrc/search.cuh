@@ -397,18 +397,57 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
     return v;
 }
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
-// Strong relaxed writes: after fence_acq_rel_gpu they form release patterns.
-__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+// Strong relaxed reads: followed by fence_acq_rel_gpu they form acquire
+// patterns.  Strong relaxed writes: after fence_acq_rel_gpu they form release
+// patterns.
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ void red_relaxed_add_u32(uint32_t* p, uint32_t v) {
     asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Waits (one thread) until the ready word *p carries iteration `target`
+// (high half >= target), given `w`, a value of *p read before and ordered by
+// an acquire fence since; returns the word in `w`.  Bounded like
+// team_wait_u32 below; returns with acquire ordering.
+__device__ __forceinline__ bool team_wait_ready(const unsigned long long* p, uint32_t target,
+                                                unsigned long long& w, TeamCtl* tc, uint64_t timeout_ns) {
+    if ((uint32_t)(w >> 32) >= target) return true;
+    const volatile uint32_t* vab = &tc->abort;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        w = ld_acquire_u64(p);
+        if ((uint32_t)(w >> 32) >= target) return true;
+        if (*vab) return false;
+        if ((spin & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+            atomicExch(&tc->abort, 1u);
+            return false;
+        }
+        if (spin > 64) __nanosleep(32);
+    }
+}
+
 // Waits (one thread) until *p >= target, given `seen`, a value of *p read
-// with acquire before: bounded by the deadline, released by the team's abort
-// flag; a timeout raises the flag.  Returns with acquire ordering: the writes
-// the waited-for block made before raising *p are visible.
+// before and ordered by an acquire fence since: bounded by the deadline,
+// released by the team's abort flag; a timeout raises the flag.  Returns with
+// acquire ordering: the writes the waited-for block made before raising *p
+// are visible.
 __device__ __forceinline__ bool team_wait_u32(const uint32_t* p, uint32_t target, uint32_t seen, TeamCtl* tc,
                                               uint64_t timeout_ns) {
     if (seen >= target) return true;
@@ -569,13 +608,12 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     // buffers and aggregates its counters and minima in shared memory; thread
     // 0 publishes them (ready word, cut slot).
     const size_t region_cap = stage_entries_per_buffer(W, d.ew, MAXN);
-    uint32_t* const ring_counts =
-        multi ? reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(tm.stage) +
-                                            (size_t)kStageRing * stage_cap * sizeof(E))
+    unsigned long long* const ready =
+        multi ? reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(tm.stage) +
+                                                      (size_t)kStageRing * stage_cap * sizeof(E))
               : nullptr;
-    uint32_t* const ready = multi ? ring_counts + (size_t)kStageRing * tm.ctas : nullptr;
     if (multi && threadIdx.x == 0) {
-        ready[rank] = 0;
+        for (uint32_t r = 0; r < kStageRing; ++r) ready[(size_t)r * tm.ctas + rank] = 0;
         if (rank == 0)
             for (uint32_t k = 0; k < kCuts; ++k) {
                 CutSlot& c = tm.ctl->cut[k];
@@ -822,13 +860,14 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
             __syncthreads();  // every warp's stage writes and counters are done
             if (threadIdx.x == 0) {
                 CutSlot* cuts = tm.ctl->cut;
-                const uint32_t row = (it % kStageRing) * tm.ctas;
+                unsigned long long* const rw = ready + (size_t)(it % kStageRing) * tm.ctas;
                 const uint32_t from = (rank + it) % tm.ctas;
-                // Both awaited words are read first: their round trips overlap
+                // Both awaited words are read first, relaxed (the fence below
+                // orders them before what follows): their round trips overlap
                 // this block's publication.
-                const uint32_t seen = ld_acquire_u32(ready + from);
+                unsigned long long wfrom = from == rank ? 0ull : ld_relaxed_u64(rw + from);
                 const CutSlot* t = cuts + (it + kCuts - kCutLag) % kCuts;
-                const uint32_t tseen = it >= kCutLag ? ld_acquire_u32(&t->count) : 0u;
+                const uint32_t tseen = it >= kCutLag ? ld_relaxed_u32(&t->count) : 0u;
                 const uint32_t lossy = sm.agg.err ? sm.agg.err : sm.agg_err_prev;
                 uint32_t err = 0;
                 if (leader) {
@@ -856,13 +895,14 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 if (sm.agg.best != kInf) atomicMin(&c->best, sm.agg.best);
                 if (lossy) atomicCAS(&c->lossy, 0u, lossy);
                 if (err) atomicCAS(&c->err, 0u, err);
-                __stcg(ring_counts + row + rank, sm.agg.count);
-                // One release fence for both arrivals: every warp's stage
-                // writes (ordered before thread 0 by the block barrier), the
-                // region count and the cut's updates precede the ready flag
-                // and the cut arrival.
+                const uint32_t mine = sm.agg.count;
+                // One fence for both arrivals and both early reads: every
+                // warp's stage writes (ordered before thread 0 by the block
+                // barrier) and the cut's updates precede the ready word and
+                // the cut arrival (release); the words read above precede
+                // everything after (acquire).
                 fence_acq_rel_gpu();
-                st_relaxed_u32(ready + rank, it + 1);
+                st_relaxed_u64(rw + rank, ((unsigned long long)(it + 1) << 32) | mine);
                 red_relaxed_add_u32(&c->count, 1u);
                 sm.agg.best = kInf;
                 sm.agg.err = 0;
@@ -871,10 +911,12 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                 sm.agg_minprio = kInfPrio;
                 sm.agg_err_prev = 0;
                 uint32_t dec = kInf, n = 0, dbest = kInf, dfmin = kInf;
-                if (!team_wait_u32(ready + from, it + 1, from == rank ? it + 1 : seen, tm.ctl, P.barrier_timeout_ns))
+                if (from == rank)
+                    n = mine;
+                else if (!team_wait_ready(rw + from, it + 1, wfrom, tm.ctl, P.barrier_timeout_ns))
                     dec = ST_BARRIER;
                 else
-                    n = __ldcg(ring_counts + row + from);
+                    n = (uint32_t)wfrom;
                 if (dec == kInf && it >= kCutLag) {
                     // Waits only while a block is more than kCutLag iterations behind.
                     if (!team_wait_u32(&t->count, tm.ctas, tseen, tm.ctl, P.barrier_timeout_ns)) {
