@@ -1173,16 +1173,47 @@ __global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
 
 // Path rebuild (a_star.h:268-281 walked one <<<1,1>>> launch per step): one
 // thread per finished instance follows parent moves from the goal to the
-// start twice -- once to count, once to write the states goal-first into a
-// slice of the shared path arena reserved with one atomic.
+// start and writes the states goal-first.  An instance that has the arena to
+// itself (a launch of one) writes as it walks; otherwise it walks twice --
+// once to count, once to write into a slice of the shared arena reserved
+// with one atomic.  Each step is a dependent table read, so one walk instead
+// of two halves the time of long paths (a 4096^2 grid's runs to ~9k steps).
 template <class D>
 __device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long long* arena,
-                          unsigned long long arena_words, unsigned long long* arena_used) {
+                          unsigned long long arena_words, unsigned long long* arena_used, bool own_arena) {
     InstCtl* ctl = d.ctl;
     const typename D::Tab tab = D::make_tab(d);
     // Every step lowers g by at least 1, so a walk longer than best + 1 states
     // means a damaged table.
     const uint64_t limit = (uint64_t)ctl->best + 2;
+    if (own_arena) {
+        const uint64_t cap = arena_words / D::KW;
+        uint64_t len = 0;
+        for (typename D::KeyT k = ctx.goal;;) {
+            if (len >= cap || len > limit) {  // the host retries with room for best + 1 states
+                ctl->status = ST_PATH_CAP;
+                ctl->path_len = 0;
+                return;
+            }
+            unsigned long long* o = arena + len * D::KW;
+            o[0] = (uint64_t)k;
+            if constexpr (D::KW == 2) o[1] = (uint64_t)(k >> 64);
+            ++len;
+            if (D::is_start(ctx, k)) break;
+            const uint64_t v = D::get(tab, k);
+            const uint32_t m = (uint32_t)v;
+            if (v == kEmpty || m == D::kRootCode) {
+                ctl->status = ST_PATH_CAP;
+                ctl->path_len = 0;
+                return;
+            }
+            k = D::parent(ctx, tab, k, m);
+        }
+        ctl->path_len = (uint32_t)len;
+        ctl->path_off = 0;
+        atomicAdd(arena_used, (unsigned long long)(len * D::KW));
+        return;
+    }
     uint64_t len = 1;
     for (typename D::KeyT k = ctx.goal; !D::is_start(ctx, k); ++len) {
         const uint64_t v = D::get(tab, k);
@@ -1227,19 +1258,19 @@ static __global__ void path_kernel(const InstDesc* insts, uint32_t n, unsigned l
         case KIND_SLIDING3: {
             SlidingDom<3>::Ctx c;
             sliding_ctx_min<3>(c, d);
-            walk_path<SlidingDom<3>>(d, c, arena, arena_words, arena_used);
+            walk_path<SlidingDom<3>>(d, c, arena, arena_words, arena_used, n == 1);
             break;
         }
         case KIND_SLIDING4: {
             SlidingDom<4>::Ctx c;
             sliding_ctx_min<4>(c, d);
-            walk_path<SlidingDom<4>>(d, c, arena, arena_words, arena_used);
+            walk_path<SlidingDom<4>>(d, c, arena, arena_words, arena_used, n == 1);
             break;
         }
         case KIND_SLIDING5: {
             SlidingDom<5>::Ctx c;
             sliding_ctx_min<5>(c, d);
-            walk_path<SlidingDom<5>>(d, c, arena, arena_words, arena_used);
+            walk_path<SlidingDom<5>>(d, c, arena, arena_words, arena_used, n == 1);
             break;
         }
         case KIND_GRID: {
@@ -1247,7 +1278,7 @@ static __global__ void path_kernel(const InstDesc* insts, uint32_t n, unsigned l
             c.W = d.W;
             c.goal = (uint32_t)d.goal0;
             c.start = (uint32_t)d.start0;
-            walk_path<GridDom>(d, c, arena, arena_words, arena_used);
+            walk_path<GridDom>(d, c, arena, arena_words, arena_used, n == 1);
             break;
         }
         default:
