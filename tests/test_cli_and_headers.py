@@ -33,3 +33,32 @@ def test_template_api_compiles():
     import build_harness
     obj = build_harness.build(obj_only=True)
     assert os.path.getsize(obj) > 0
+
+
+def test_python_structs_match_the_c_header(tmp_path):
+    """The ctypes mirrors of the C ABI's structs have the header's sizes and
+    field offsets (gcc on include/gastar.h; no GPU)."""
+    import ctypes as C
+    sys.path.insert(0, ROOT)
+    from cuda_a_star_gb300 import _lib
+    structs = {"gastar_config": _lib.Config, "gastar_result": _lib.Result,
+               "gastar_batch_config": _lib.BatchConfig}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gastar.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, field, val = line.split()
+        got[(cname, field)] = int(val)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
