@@ -741,18 +741,24 @@ bool cache_lookup(const char* path, const std::string& sig, gastar_batch_config&
     return found;
 }
 
-// Device time of one trial batch over `idx` with configuration `cfg`.
-// The sample runs on the same share of the GPU as it is of the batch, so
-// that blocks per instance -- which decides whether teams pay -- match the
-// full run.
+// Estimated device time of the full batch from one trial batch over `idx`
+// with configuration `cfg`.  The sample's persistent launch runs on the same
+// share of the GPU as the sample is of the batch, so that blocks per instance
+// -- which decides whether teams pay -- and the launch's time match the full
+// run.  Its overflow re-runs and plain re-solves use the whole GPU, as they do
+// in the full run, where there are 1 / share times as many of them: that part
+// is scaled up accordingly (a configuration that overflows more is not
+// favoured because the sample has few overflows).
 int trial(gastar_batch* b, const std::vector<uint32_t>& idx, const gastar_batch_config& cfg, float& ms) {
     gastar_batch* t = gastar_batch_create(b->ctx, &cfg);
     if (!t) return GASTAR_OUT_OF_MEMORY;
     t->cfg.use_graph = 0;
-    t->block_share = std::min(1.0, (double)idx.size() / (double)b->insts.size());
+    const double share = std::min(1.0, (double)idx.size() / (double)b->insts.size());
+    t->block_share = share;
     for (uint32_t i : idx) t->insts.push_back(b->insts[i]);
     const int rc = gastar_batch_run(t);
-    ms = t->kernel_ms;
+    const double after = (double)t->retry_ms + (double)t->promote_ms;
+    ms = (float)((double)t->kernel_ms - after + after / share);
     for (uint32_t j = 0; rc == GASTAR_OK && j < idx.size(); ++j)
         if (t->h_ctl[j].status != ST_OK && t->h_ctl[j].status != ST_NO_PATH) ms = 1e30f;  // unusable
     gastar_batch_destroy(t);
