@@ -58,11 +58,21 @@ int device_min_weight(gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStr
 
 using namespace gastar;
 
+struct gastar_batch;
+namespace gastar {
+uint8_t* grid_alloc(gastar_batch* b, size_t bytes);
+}
+
 struct gastar_batch {
     gastar_ctx* ctx = nullptr;
     gastar_batch_config cfg;
     std::vector<Problem> insts;
-    std::vector<uint64_t> weights_off;
+    // Grid weights, copied to the device when the grid is added: bump
+    // allocation in chunks of at least 256 MiB, freed with the batch.
+    // Re-run batches and autotuner trials point at their parent's copies.
+    std::vector<void*> grid_chunks;
+    size_t grid_chunk_used = 0, grid_chunk_cap = 0;
+    uint64_t grid_bytes = 0, grid_h2d = 0;
     std::vector<uint8_t> heavy;        // solved by a multi-block team
     std::vector<uint8_t> promotable;   // re-solved by the plain engine past the budget
     uint32_t n_heavy = 0, heavy_teams = 0;
@@ -77,7 +87,7 @@ struct gastar_batch {
     gastar_batch* sub = nullptr;    // re-run batch of the last run's overflowed instances,
     std::vector<uint32_t> sub_idx;  // kept while the same instances overflow
     bool uploaded = false;
-    DevBuf arena, weights, descs, ctls, order, counters, paths;
+    DevBuf arena, descs, ctls, order, counters, paths;
     std::vector<InstDesc> h_desc;
     std::vector<uint64_t> tl_start, tl_end;  // the persistent launch's schedule (globaltimer ns)
     InstCtl* h_ctl = nullptr;               // pinned, n + 1 (last = arena counter)
@@ -90,6 +100,29 @@ struct gastar_batch {
     uint64_t h2d = 0, d2h = 0, device_bytes = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
+
+namespace gastar {
+
+uint8_t* grid_alloc(gastar_batch* b, size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (b->grid_chunks.empty() || b->grid_chunk_used + bytes > b->grid_chunk_cap) {
+        const size_t cap = std::max<size_t>(bytes, (size_t)256 << 20);
+        void* c = nullptr;
+        if (cudaMalloc(&c, cap) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        b->grid_chunks.push_back(c);
+        b->grid_chunk_cap = cap;
+        b->grid_chunk_used = 0;
+        b->grid_bytes += cap;
+    }
+    uint8_t* r = static_cast<uint8_t*>(b->grid_chunks.back()) + b->grid_chunk_used;
+    b->grid_chunk_used += bytes;
+    return r;
+}
+
+}  // namespace gastar
 
 extern "C" {
 
@@ -134,7 +167,7 @@ void gastar_batch_destroy(gastar_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     gastar_batch_destroy(b->sub);
     b->arena.release();
-    b->weights.release();
+    for (void* c : b->grid_chunks) cudaFree(c);
     b->descs.release();
     b->ctls.release();
     b->order.release();
@@ -159,14 +192,33 @@ int gastar_batch_add_sliding(gastar_batch* b, uint32_t n, const uint8_t* start, 
     return (int)b->insts.size() - 1;
 }
 
+// The grid goes straight from the caller's buffer to the device (no host
+// copy: first-touch page faults of a host copy cost more than the transfer),
+// and its least passable weight is reduced there.
 int gastar_batch_add_grid(gastar_batch* b, uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx,
                           uint32_t sy, uint32_t tx, uint32_t ty) {
     if (!b || b->uploaded) return -GASTAR_BAD_INPUT;
     Problem p;
-    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, b->cfg.heuristic, p)) {
+    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, b->cfg.heuristic, p, false)) {
         set_error("grid: bad dimensions or endpoints");
         return -GASTAR_BAD_INPUT;
     }
+    if (cudaSetDevice(b->ctx->device) != cudaSuccess) return -GASTAR_CUDA_ERROR;
+    const size_t cells = (size_t)w * h;
+    uint8_t* d = grid_alloc(b, cells);
+    if (!d) {
+        set_error("batch: grid weights exceed free device memory");
+        return -GASTAR_OUT_OF_MEMORY;
+    }
+    cudaStream_t st = b->ctx->stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, weights, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+        return -GASTAR_CUDA_ERROR;
+    uint32_t mw = 255;
+    const int rc = device_min_weight(b->ctx, d, cells, st, &mw);
+    if (rc != GASTAR_OK) return -rc;
+    set_grid_minw(p, mw, b->cfg.heuristic);
+    p.d_weights = d;
+    b->grid_h2d += cells;
     b->insts.push_back(std::move(p));
     return (int)b->insts.size() - 1;
 }
@@ -263,39 +315,32 @@ int batch_upload(gastar_batch* b) {
     }
     std::vector<PartPlan> plans(n);
     std::vector<uint64_t> part_off(n);
-    uint64_t arena_bytes = 0, weights_bytes = 0;
+    uint64_t arena_bytes = 0;
     b->path_words = 0;
-    b->weights_off.assign(n, 0);
     for (uint32_t i = 0; i < n; ++i) {
         plans[i] = plan_partition(b->insts[i], b->heavy[i] ? pch : pc);
         part_off[i] = arena_bytes;
         arena_bytes += plans[i].bytes;
         b->path_words += plans[i].path_words;
-        if (b->insts[i].kind == KIND_GRID) {
-            weights_bytes = (weights_bytes + 15) & ~15ull;
-            b->weights_off[i] = weights_bytes;
-            weights_bytes += b->insts[i].weights.size();
-        }
     }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    if (arena_bytes + weights_bytes + (64ull << 20) > free_b) {
+    if (arena_bytes + (64ull << 20) > free_b) {
         set_error("batch partitions exceed free device memory");
         return GASTAR_OUT_OF_MEMORY;
     }
-    if (!b->arena.ensure(arena_bytes) || !b->weights.ensure(std::max<uint64_t>(weights_bytes, 16)) ||
-        !b->descs.ensure(sizeof(InstDesc) * n) || !b->ctls.ensure(sizeof(InstCtl) * (n + 1)) ||
+    if (!b->arena.ensure(arena_bytes) || !b->descs.ensure(sizeof(InstDesc) * n) || !b->ctls.ensure(sizeof(InstCtl) * (n + 1)) ||
         !b->order.ensure(sizeof(uint32_t) * n) || !b->counters.ensure(64) ||
         !b->paths.ensure(b->path_words * 8))
         return GASTAR_OUT_OF_MEMORY;
-    b->device_bytes = arena_bytes + weights_bytes + b->path_words * 8 +
+    b->device_bytes = arena_bytes + b->grid_bytes + b->path_words * 8 +
                       (sizeof(InstDesc) + sizeof(InstCtl)) * (size_t)n;
     char* base = reinterpret_cast<char*>(b->arena.p);
     InstCtl* ctl_base = reinterpret_cast<InstCtl*>(b->ctls.p);
     b->h_desc.assign(n, InstDesc());
     for (uint32_t i = 0; i < n; ++i) {
         fill_desc(b->h_desc[i], b->insts[i], b->heavy[i] ? pch : pc, plans[i], base + part_off[i],
-                  reinterpret_cast<const uint8_t*>(b->weights.p) + b->weights_off[i], ctl_base + i);
+                  b->insts[i].d_weights, ctl_base + i);
         if (b->promotable[i])
             b->h_desc[i].max_exp = b->h_desc[i].max_exp ? std::min<uint64_t>(b->h_desc[i].max_exp,
                                                                               b->cfg.promote_expansions)
@@ -323,16 +368,7 @@ int batch_upload(gastar_batch* b) {
     if (!b->h_ctl && !cuda_ok(cudaMallocHost(&b->h_ctl, sizeof(InstCtl) * (n + 1)), "cudaMallocHost"))
         return GASTAR_CUDA_ERROR;
     cudaStream_t st = c->stream;
-    b->h2d = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        const Problem& in = b->insts[i];
-        if (in.kind != KIND_GRID) continue;
-        if (!cuda_ok(cudaMemcpyAsync(reinterpret_cast<char*>(b->weights.p) + b->weights_off[i],
-                                     in.weights.data(), in.weights.size(), cudaMemcpyHostToDevice, st),
-                     "cudaMemcpyAsync"))
-            return GASTAR_CUDA_ERROR;
-        b->h2d += in.weights.size();
-    }
+    b->h2d = b->grid_h2d;  // the grids went up when they were added
     if (!cuda_ok(cudaMemcpyAsync(b->descs.p, b->h_desc.data(), sizeof(InstDesc) * n,
                                  cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
         (!order.empty() && !cuda_ok(cudaMemcpyAsync(b->order.p, order.data(), sizeof(uint32_t) * order.size(),
@@ -528,7 +564,7 @@ static int batch_promote(gastar_batch* b) {
             pp.W = p.W;
             pp.H = p.H;
             pp.minw = p.minw;
-            pp.d_weights = reinterpret_cast<const uint8_t*>(b->weights.p) + b->weights_off[i];
+            pp.d_weights = p.d_weights;
         }
         gastar_config cfg;
         gastar_config_default(&cfg);

@@ -54,7 +54,7 @@ uint8_t min_passable_weight(const uint8_t* q, size_t cells) {
 }
 
 bool make_grid_problem(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx, uint32_t sy,
-                       uint32_t tx, uint32_t ty, uint32_t heuristic, Problem& p) {
+                       uint32_t tx, uint32_t ty, uint32_t heuristic, Problem& p, bool host_copy) {
     if (!weights || !w || !h || w > 65535 || h > 65535 || sx >= w || sy >= h || tx >= w || ty >= h)
         return false;
     p = Problem();
@@ -64,11 +64,18 @@ bool make_grid_problem(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t 
     p.start0 = (uint64_t)sy * w + sx;
     p.goal0 = (uint64_t)ty * w + tx;
     const size_t cells = (size_t)w * h;
-    p.minw = min_passable_weight(weights, cells);  // the caller's buffer: still warm
-    p.weights.assign(weights, weights + cells);
-    p.f0 = grid_h(sx, sy, tx, ty, p.minw, heuristic);
     p.est = 80ull * cells;
+    if (!host_copy) return true;
+    p.weights.assign(weights, weights + cells);
+    set_grid_minw(p, min_passable_weight(weights, cells), heuristic);
     return true;
+}
+
+void set_grid_minw(Problem& p, uint32_t minw, uint32_t heuristic) {
+    p.minw = minw;
+    const uint32_t sx = (uint32_t)(p.start0 % p.W), sy = (uint32_t)(p.start0 / p.W);
+    const uint32_t tx = (uint32_t)(p.goal0 % p.W), ty = (uint32_t)(p.goal0 / p.W);
+    p.f0 = grid_h(sx, sy, tx, ty, minw, heuristic);
 }
 
 PartPlan plan_partition(const Problem& p, const PartConfig& c) {

@@ -15,7 +15,8 @@ struct Problem {
     uint64_t start0 = 0, start1 = 0, goal0 = 0, goal1 = 0;
     uint32_t W = 0, H = 0, minw = 0, f0 = 0;
     bool unreachable = false;      // other parity class of the standard sliding moves
-    std::vector<uint8_t> weights;  // grid
+    std::vector<uint8_t> weights;  // grid, host copy (served requests)
+    const uint8_t* d_weights = nullptr;  // grid, device copy (batched instances; owned by the batch)
     uint64_t est = 0;              // expected one-block search time in ns
 };
 
@@ -57,8 +58,12 @@ struct PartPlan {
 
 bool make_sliding_problem(uint32_t n, const uint8_t* start, const uint8_t* goal, uint32_t heuristic,
                           uint32_t moves, Problem& p);
+// With host_copy false the weights are neither copied nor scanned: the caller
+// places them (on the device) and sets the least weight with set_grid_minw.
 bool make_grid_problem(uint32_t w, uint32_t h, const uint8_t* weights, uint32_t sx, uint32_t sy,
-                       uint32_t tx, uint32_t ty, uint32_t heuristic, Problem& p);
+                       uint32_t tx, uint32_t ty, uint32_t heuristic, Problem& p, bool host_copy = true);
+// Least passable weight of a grid problem (255: none) and the start's f.
+void set_grid_minw(Problem& p, uint32_t minw, uint32_t heuristic);
 PartPlan plan_partition(const Problem& p, const PartConfig& c);
 // Fills an instance descriptor for a partition placed at `base` (256-byte
 // aligned).  `d_weights` is used for grids unless the partition owns them.
