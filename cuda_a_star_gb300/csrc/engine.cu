@@ -23,15 +23,18 @@
 namespace gastar {
 
 // Launch block of a plain solve (one device allocation, one upload):
-// descriptor | control block | team control | work counter | path counter.
+// descriptor | control block | work counter | path counter | team control.
+// The upload ends after the team control's first line (barrier counter,
+// abort flag): the team's first block clears the cut slots itself.
 constexpr size_t kLbAlign = 128;
 constexpr size_t lb_round(size_t x) { return (x + kLbAlign - 1) / kLbAlign * kLbAlign; }
 constexpr size_t kLbDesc = 0;
 constexpr size_t kLbCtl = lb_round(sizeof(InstDesc));
-constexpr size_t kLbTeam = kLbCtl + lb_round(sizeof(InstCtl));
-constexpr size_t kLbNext = kLbTeam + lb_round(sizeof(TeamCtl));
+constexpr size_t kLbNext = kLbCtl + lb_round(sizeof(InstCtl));
 constexpr size_t kLbUsed = kLbNext + kLbAlign;
-constexpr size_t kLbBytes = kLbUsed + kLbAlign;
+constexpr size_t kLbTeam = kLbUsed + kLbAlign;
+constexpr size_t kLbBytes = kLbTeam + lb_round(sizeof(TeamCtl));
+constexpr size_t kLbUpload = kLbTeam + kLbAlign;
 constexpr uint64_t kPathPrefixWords = 1024;   // path words read back with the control block
 constexpr uint64_t kPathArenaWords = 1 << 16;  // first path arena of a puzzle solve
 
@@ -511,8 +514,8 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     P.stage = c->stage.p;
     P.barrier_timeout_ns = 2000000000ull;
 
-    GA_CUDA(cudaMemcpyAsync(lb, hl, kLbBytes, cudaMemcpyHostToDevice, st));
-    as.h2d += kLbBytes;
+    GA_CUDA(cudaMemcpyAsync(lb, hl, kLbUpload, cudaMemcpyHostToDevice, st));
+    as.h2d += kLbUpload;
     GA_CUDA(cudaEventRecord(c->e0, st));
     int rc = launch_search(c, kinds, P, (uint32_t)blocks, threads, smem, st);
     if (rc != GASTAR_OK) return rc;

@@ -1,6 +1,7 @@
 // Host/device shared descriptors of the GA* engine.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 
 #if !defined(__CUDACC__) && !defined(__host__)
@@ -128,15 +129,23 @@ constexpr uint32_t kSlots = 4;
 
 // Control of a multi-block team (one instance on many blocks).
 // One cut of a multi-block team: the state at the start of an iteration.
-struct alignas(16) CutSlot {
+// Every block updates the minimum, the two counts and the arrival count of a
+// slot with atomics in the same few hundred nanoseconds: each of them has its
+// own 128-byte line, so those atomics queue at different L2 slices.
+struct alignas(128) CutSlot {
     unsigned long long minprio;  // min priority over the team's heaps
-    unsigned long long claims;   // table slots the blocks claimed since their last cut
-    unsigned long long exps;     // expansions since the blocks' last cut
     uint32_t best;               // goal costs found in the iteration before
     uint32_t lossy;              // entries were lost (table or heap full, cost range)
     uint32_t err;                // budget or timeout
+    uint32_t pad0[27];
+    unsigned long long claims;   // table slots the blocks claimed since their last cut
+    uint32_t pad1[30];
+    unsigned long long exps;     // expansions since the blocks' last cut
+    uint32_t pad2[30];
     uint32_t count;              // blocks that published
+    uint32_t pad3[31];
 };
+static_assert(sizeof(CutSlot) == 512, "one 128-byte line per contended word");
 
 // The barrier counter only grows (barrier k of a team ends when it reaches
 // (k+1) x blocks) and sits on its own 128-byte line, apart from the cut slots
@@ -147,6 +156,7 @@ struct alignas(128) TeamCtl {
     uint32_t pad[28];
     CutSlot cut[kCuts];
 };
+static_assert(offsetof(TeamCtl, cut) == 128, "the barrier counter and abort flag fill the first line");
 inline void team_ctl_init(TeamCtl& t) {
     t.arrive = 0;
     t.abort = 0;
