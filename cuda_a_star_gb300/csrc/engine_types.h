@@ -38,7 +38,11 @@ inline __host__ __device__ size_t stage_entries_per_buffer(uint32_t heaps, uint3
 constexpr uint32_t kStageRing = 4;
 constexpr uint32_t kCutLag = 2;
 constexpr uint32_t kCuts = 16;  // cut slots in the ring (> 3 * kCutLag + 2)
-static_assert(kStageRing > kCutLag, "a stage buffer must be consumed before it is reused");
+// A block writes stage buffer i % kStageRing (and its ready words) in
+// iteration i only after cut i - 1 - kCutLag is complete, i.e. after every
+// block's push of iteration i - 2 - kCutLag: the buffer's previous use,
+// iteration i - kStageRing, must be no later than that.
+static_assert(kStageRing >= kCutLag + 2, "a stage buffer must be consumed before it is reused");
 
 constexpr uint32_t kSlotsHost = 4;
 
