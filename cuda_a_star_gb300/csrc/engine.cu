@@ -123,7 +123,8 @@ uint32_t fit_heap_snodes(gastar_ctx* c, uint32_t kinds, uint32_t warps, uint32_t
     return cand;
 }
 
-int occupancy_blocks(gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem) {
+int occupancy_blocks(gastar_ctx* /*c: the current device's context*/, uint32_t kinds, uint32_t threads,
+                     size_t smem) {
     const void* f = search_kernel_for(kinds, threads);
     if (smem > 48 * 1024)
         if (!cuda_ok(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -136,8 +137,8 @@ int occupancy_blocks(gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t sme
     return nb;
 }
 
-int launch_search(gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
-                  uint32_t threads, size_t smem, cudaStream_t st) {
+int launch_search(gastar_ctx* /*c: the current device's context*/, uint32_t kinds, const LaunchParams& P,
+                  uint32_t blocks, uint32_t threads, size_t smem, cudaStream_t st) {
     const void* f = search_kernel_for(kinds, threads);
     if (smem > 48 * 1024)
         GA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
