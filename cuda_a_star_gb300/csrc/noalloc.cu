@@ -16,14 +16,15 @@
 // Every call uses the same array and the array keeps the previous call's
 // contents; the search clears its table and control words itself.  Calls that
 // overlap on the GPU (two host threads, or two streams) race on the array and
-// must be serialised by the caller.  The first call on a device looks up the
-// array's device address (cudaGetSymbolAddress) with that device current; make
-// that first call before any stream capture begins.
+// must be serialised by the caller.  In host code the array's name is only a
+// host-side stand-in, so every call looks up the array's device address with
+// cudaGetSymbolAddress on the device that is current: the lookup resolves
+// against the current context, so it stays right after a cudaDeviceReset.
+// The call synchronises the stream it runs on before it returns.
 #include <cuda_runtime.h>
 
 #include <chrono>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/gastar.h"
 #include "engine_internal.h"
@@ -55,26 +56,14 @@ static_assert(kTableOff % 256 == 0 && kHeapOff % 256 == 0, "alignment");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (set up once).
+// Device address of the scratch array in the current context.  Looked up on
+// every call: a cached address would go stale when the caller resets the
+// device or destroys its primary context and the module is loaded again.
 int scratch_for_current_device(void** out) {
-    int dev = 0;
-    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return GASTAR_CUDA_ERROR;
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_error("gastar_solve_sliding_noalloc: device index above 63");
-        return GASTAR_NO_DEVICE;
-    }
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-        void* p = nullptr;
-        if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress"))
-            return GASTAR_CUDA_ERROR;
-        g_scratch[dev] = p;
-    }
-    *out = g_scratch[dev];
+    void* p = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress"))
+        return GASTAR_CUDA_ERROR;
+    *out = p;
     return GASTAR_OK;
 }
 
@@ -185,6 +174,23 @@ extern "C" int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t* start, co
             (e = cudaStreamSynchronize(st)) != cudaSuccess)
             return fail(e, "path");
         out->d2h_bytes += sizeof(ctl);
+    }
+    if (ctl.status == ST_PATH_CAP && ctl.best != kInf) {
+        // The goal was reached but its path is longer than the arena of
+        // kPathWords states (possible only with the inadmissible heuristic):
+        // the cost stands, the path is not returned.  Every move costs 1, so
+        // the path needs best + 1 states.
+        out->status = GASTAR_PATH_CAP;
+        out->cost = ctl.best;
+        out->path_len = ctl.best + 1;
+        out->iterations = ctl.iterations;
+        out->expansions = ctl.expansions;
+        out->generated = ctl.generated;
+        out->pushes = ctl.pushes;
+        out->stale = ctl.stale;
+        out->table_used = ctl.table_used;
+        out->attempts = 1;
+        return finish();
     }
     out->status = (int32_t)ctl.status;
     out->cost = ctl.status == ST_OK ? ctl.best : 0;

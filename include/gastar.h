@@ -133,12 +133,22 @@ int gastar_solve_grid_device(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint
 /* 8-puzzle solve that allocates nothing, for callers that cannot call
  * cudaMalloc (their device memory is reserved by another pool, or they must
  * avoid the device-wide synchronisation of cudaMalloc/cudaFree).  No
- * counterpart in the reference.  Same arguments and results as
- * gastar_solve_sliding without a context; n must be 3 (GASTAR_BAD_INPUT
+ * counterpart in the reference.  Arguments and result fields as
+ * gastar_solve_sliding, without a context; n must be 3 (GASTAR_BAD_INPUT
  * otherwise).  Scratch is a fixed ~16 MiB device array inside the library,
  * held by every GPU that loads the library until exit; all calls share it, so
- * calls that overlap on the GPU race.  The first call on a device looks up the
- * array's address: make it before any stream capture.  kernel_ms is 0. */
+ * calls that overlap on the GPU race.  Every call looks up the array's address
+ * on the current device, and synchronises the stream it runs on (cfg->stream,
+ * or the legacy default stream when that is NULL) before it returns.
+ * Fixed shape: one block of 4 warp-heaps popping 32 entries each, a 2^19-slot
+ * table, 4095 nodes per warp-heap, a 4096-state path arena, no regrow; the
+ * config fields num_queues, expansion_width, warps_per_block, max_blocks,
+ * load_factor, table_log2, heap_entries, regrow and open_list are ignored
+ * (heuristic, moves, max_expansions, max_iterations, timeout_ms, delta and
+ * stream apply).  Costs equal gastar_solve_sliding's for the admissible and
+ * zero heuristics (both optimal); with GASTAR_H_REFERENCE the cost depends on
+ * the expansion order and may differ.  A path longer than the arena returns
+ * GASTAR_PATH_CAP with the cost and path_len = cost + 1.  kernel_ms is 0. */
 int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t *start, const uint8_t *goal,
                                  const gastar_config *cfg, uint8_t *path, uint32_t path_cap,
                                  gastar_result *out);
