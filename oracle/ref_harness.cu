@@ -1,6 +1,6 @@
 // Golden-vector harness over the reference's own host-reachable functions.
 //
-// TEST INFRASTRUCTURE ONLY.  Built by oracle/build_ref.py from the reference
+// TEST INFRASTRUCTURE ONLY.  Built by `oracle/build.py --ref` from the reference
 // headers where they lie (passed with -I); the binary goes to oracle/_ref/ and
 // runs in the development container only.  It is how the oracle's
 // restatement is pinned: tests/golden/make_golden.py runs it and stores its
