@@ -170,6 +170,24 @@ class Engine:
                                                 C.byref(gbs), C.byref(ms)), "random_access_peak")
         return {"kind": kind, "gbs": gbs.value, "ms": ms.value}
 
+    def random_access_sweep(self, kinds=("gather", "cas"),
+                            buffers=(64 << 20, 256 << 20, 1 << 30, 4 << 30, 16 << 30),
+                            in_flight=(2, 4, 8, 16, 32), loads_per_sector=(1, 2)) -> list[dict]:
+        """The random 32-byte-sector rate over buffer size, accesses in flight
+        per thread and (gather) 16-byte loads per sector: one row per point."""
+        rows = []
+        for kind in kinds:
+            k = 0 if kind == "gather" else 1
+            for b in buffers:
+                for f in in_flight:
+                    for lp in (loads_per_sector if k == 0 else (1,)):
+                        gbs, ms = C.c_double(), C.c_double()
+                        _check(lib().gastar_measure_random_peak_ex(self._h, b, k, f, lp, C.byref(gbs),
+                                                                   C.byref(ms)), "random_access_sweep")
+                        rows.append({"kind": kind, "buffer_bytes": b, "in_flight": f,
+                                     "loads_per_sector": lp, "gbs": gbs.value, "ms": ms.value})
+        return rows
+
     def batch(self, **kw) -> "Batch":
         return Batch(self, **kw)
 

@@ -28,7 +28,7 @@ EXPORTS = [
     "gastar_parse_sliding", "gastar_format_sliding", "gastar_parse_grid_dims",
     "gastar_parse_grid", "gastar_gen_sliding", "gastar_gen_grid",
     "gastar_format_grid", "gastar_encode_grid_binary", "gastar_decode_grid_header",
-    "gastar_decode_grid_binary", "gastar_measure_random_peak",
+    "gastar_decode_grid_binary", "gastar_measure_random_peak", "gastar_measure_random_peak_ex",
 ]
 
 
@@ -157,6 +157,9 @@ def load(path: str | None = None) -> C.CDLL:
         "gastar_decode_grid_header": (C.c_int, [u8p, C.c_size_t, u32p, u32p]),
         "gastar_measure_random_peak": (C.c_int, [vp, C.c_uint64, C.c_uint32,
                                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "gastar_measure_random_peak_ex": (C.c_int, [vp, C.c_uint64, C.c_uint32, C.c_uint32,
+                                                    C.c_uint32, C.POINTER(C.c_double),
+                                                    C.POINTER(C.c_double)]),
         "gastar_decode_grid_binary": (C.c_int, [u8p, C.c_size_t, u8p, C.c_size_t, u32p, u32p,
                                                 u32p, u32p]),
     }

@@ -34,7 +34,8 @@ def sources() -> list[str]:
 
 def headers() -> list[str]:
     return sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
-                  glob.glob(os.path.join(ROOT, "include", "*.h")))
+                  glob.glob(os.path.join(ROOT, "include", "*.h")) +
+                  glob.glob(os.path.join(ROOT, "include", "gastar", "*.cuh")))
 
 
 def _stale(target: str, deps: list[str]) -> bool:

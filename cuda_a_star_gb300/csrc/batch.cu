@@ -88,6 +88,7 @@ struct gastar_batch {
     std::vector<uint32_t> sub_idx;  // kept while the same instances overflow
     bool uploaded = false;
     DevBuf arena, descs, ctls, order, counters, paths;
+    DevBuf tcounts;  // per instance: length of its partition's claim list
     std::vector<InstDesc> h_desc;
     std::vector<uint64_t> tl_start, tl_end;  // the persistent launch's schedule (globaltimer ns)
     InstCtl* h_ctl = nullptr;               // pinned, n + 1 (last = arena counter)
@@ -173,6 +174,7 @@ void gastar_batch_destroy(gastar_batch* b) {
     b->order.release();
     b->counters.release();
     b->paths.release();
+    b->tcounts.release();
     b->team_ctl.release();
     b->team_stage.release();
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -244,6 +246,7 @@ PartConfig part_config(const gastar_batch* b) {
     pc.retry_level = b->retry_level;
     pc.heap_snodes = b->heap_snodes;
     pc.buckets = cf.open_list == 1;
+    pc.claim_list = true;  // re-runs clear only the slots the last search claimed
     return pc;
 }
 
@@ -331,16 +334,17 @@ int batch_upload(gastar_batch* b) {
     }
     if (!b->arena.ensure(arena_bytes) || !b->descs.ensure(sizeof(InstDesc) * n) || !b->ctls.ensure(sizeof(InstCtl) * (n + 1)) ||
         !b->order.ensure(sizeof(uint32_t) * n) || !b->counters.ensure(64) ||
-        !b->paths.ensure(b->path_words * 8))
+        !b->paths.ensure(b->path_words * 8) || !b->tcounts.ensure(sizeof(unsigned long long) * n))
         return GASTAR_OUT_OF_MEMORY;
     b->device_bytes = arena_bytes + b->grid_bytes + b->path_words * 8 +
                       (sizeof(InstDesc) + sizeof(InstCtl)) * (size_t)n;
     char* base = reinterpret_cast<char*>(b->arena.p);
     InstCtl* ctl_base = reinterpret_cast<InstCtl*>(b->ctls.p);
+    unsigned long long* tcount = reinterpret_cast<unsigned long long*>(b->tcounts.p);
     b->h_desc.assign(n, InstDesc());
     for (uint32_t i = 0; i < n; ++i) {
         fill_desc(b->h_desc[i], b->insts[i], b->heavy[i] ? pch : pc, plans[i], base + part_off[i],
-                  b->insts[i].d_weights, ctl_base + i);
+                  b->insts[i].d_weights, ctl_base + i, tcount + i);
         if (b->promotable[i])
             b->h_desc[i].max_exp = b->h_desc[i].max_exp ? std::min<uint64_t>(b->h_desc[i].max_exp,
                                                                               b->cfg.promote_expansions)
@@ -369,6 +373,10 @@ int batch_upload(gastar_batch* b) {
         return GASTAR_CUDA_ERROR;
     cudaStream_t st = c->stream;
     b->h2d = b->grid_h2d;  // the grids went up when they were added
+    // The partitions' contents are unknown: every claim-list length starts
+    // above its capacity, so each table's first search clears it whole.
+    if (!cuda_ok(cudaMemsetAsync(b->tcounts.p, 0xff, sizeof(unsigned long long) * n, st), "cudaMemsetAsync"))
+        return GASTAR_CUDA_ERROR;
     if (!cuda_ok(cudaMemcpyAsync(b->descs.p, b->h_desc.data(), sizeof(InstDesc) * n,
                                  cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
         (!order.empty() && !cuda_ok(cudaMemcpyAsync(b->order.p, order.data(), sizeof(uint32_t) * order.size(),

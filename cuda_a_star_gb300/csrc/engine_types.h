@@ -102,7 +102,11 @@ struct alignas(16) InstDesc {
     uint32_t* touched;
     unsigned long long* touched_count;
     uint64_t touched_cap;
-    uint32_t prev_slot_words, pad1;
+    uint32_t prev_slot_words;
+    // 1: the list refers to this same table, which a whole-table clear may
+    // replace when the list is long (batch partitions); 0: always the list
+    // (the plain engine's buffer may have held a larger table before).
+    uint32_t clear_either;
     uint64_t start_hi[2], goal_hi[2];  // key words 2..3 (generic plugin states)
     // Bucket front of the open list (bq_pages == 0 -> heaps only): per warp
     // bq_pages pages of 32 entries at bq_base, then the heaps' page links

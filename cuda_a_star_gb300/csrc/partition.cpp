@@ -112,6 +112,14 @@ PartPlan plan_partition(const Problem& p, const PartConfig& c) {
         pl.bq_off = (end + 255) & ~255ull;
         end = pl.bq_off + bucket_area_bytes(c.warps, pl.bq_pages, entry_bytes(p.kind));
     }
+    if (p.kind != KIND_GRID && c.claim_list) {
+        // Claims stop within two iterations past the limit; every warp may
+        // leave one chunk partly unused (as the plain engine's list).
+        pl.touched_cap = pl.table_limit + 2ull * c.warps * c.ew * max_neighbours(p.kind) +
+                         (uint64_t)c.warps * kTouchedChunk + 16;
+        pl.touched_off = (end + 255) & ~255ull;
+        end = pl.touched_off + pl.touched_cap * 4;
+    }
     if (p.kind == KIND_GRID && c.own_weights) {
         pl.weights_off = (end + 255) & ~255ull;
         end = pl.weights_off + (uint64_t)p.W * p.H;
@@ -121,7 +129,7 @@ PartPlan plan_partition(const Problem& p, const PartConfig& c) {
 }
 
 void fill_desc(InstDesc& d, const Problem& p, const PartConfig& c, const PartPlan& pl, char* base,
-               const uint8_t* d_weights, InstCtl* ctl) {
+               const uint8_t* d_weights, InstCtl* ctl, unsigned long long* touched_count) {
     std::memset(&d, 0, sizeof(d));
     d.kind = p.kind;
     d.heuristic = c.heuristic;
@@ -155,6 +163,13 @@ void fill_desc(InstDesc& d, const Problem& p, const PartConfig& c, const PartPla
     d.ctl = ctl;
     if (p.kind == KIND_GRID)
         d.weights = c.own_weights ? reinterpret_cast<const uint8_t*>(base + pl.weights_off) : d_weights;
+    if (pl.touched_cap && touched_count) {
+        d.touched = reinterpret_cast<uint32_t*>(base + pl.touched_off);
+        d.touched_count = touched_count;
+        d.touched_cap = pl.touched_cap;
+        d.prev_slot_words = key_words(p.kind) == 1 ? 2 : 4;
+        d.clear_either = 1;  // the list always refers to this partition's table
+    }
 }
 
 }  // namespace gastar

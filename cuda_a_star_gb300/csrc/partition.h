@@ -44,9 +44,12 @@ struct PartConfig {
     uint32_t heap_snodes = kHeapSmemNodes;  // heap nodes below this index live in shared memory
     bool buckets = false;         // bucket front in front of the warp-heaps
     bool own_weights = false;     // grid weights live inside the partition
+    bool claim_list = false;      // puzzles: record claimed slots so that the next search
+                                  // in the same partition clears only those
 };
 
-// Byte layout of one partition: table | heap headers | heap nodes | bucket area | weights.
+// Byte layout of one partition:
+// table | heap headers | heap nodes | bucket area | claim list | weights.
 struct PartPlan {
     uint64_t table_words = 0, table_mask = 0, table_limit = 0;
     uint32_t heap_cap = 0;
@@ -54,6 +57,8 @@ struct PartPlan {
     uint64_t bq_off = 0;          // bucket area (pages, links, free stacks)
     uint32_t bq_pages = 0;        // pages per warp (0 = no buckets)
     uint64_t path_words = 0;      // path-arena share
+    uint64_t touched_off = 0;     // claim list (u32 word offsets of claimed slots)
+    uint64_t touched_cap = 0;     // its capacity in entries (0 = no claim list)
 };
 
 bool make_sliding_problem(uint32_t n, const uint8_t* start, const uint8_t* goal, uint32_t heuristic,
@@ -67,7 +72,10 @@ void set_grid_minw(Problem& p, uint32_t minw, uint32_t heuristic);
 PartPlan plan_partition(const Problem& p, const PartConfig& c);
 // Fills an instance descriptor for a partition placed at `base` (256-byte
 // aligned).  `d_weights` is used for grids unless the partition owns them.
+// `touched_count` is the claim list's length word when the plan has a claim
+// list: above the list's capacity (the value the host sets for memory whose
+// contents are unknown) it makes the next search clear the whole table.
 void fill_desc(InstDesc& d, const Problem& p, const PartConfig& c, const PartPlan& plan, char* base,
-               const uint8_t* d_weights, InstCtl* ctl);
+               const uint8_t* d_weights, InstCtl* ctl, unsigned long long* touched_count = nullptr);
 
 }  // namespace gastar

@@ -559,12 +559,18 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     bool have_prev;          // the previous iteration's slot holds the heaps' min
     if (life == LIFE_FRESH) {
         // Clear the table (0xff = empty key and value) across the whole team:
-        // only the slots the previous solve claimed when they were recorded,
-        // otherwise the whole table.
+        // only the slots the previous solve claimed when they were recorded
+        // (a length above the list's capacity means they were not) and few,
+        // otherwise the whole table.  Listed offsets are the previous solve's, in the
+        // same buffer; its table may have been larger than this solve's.
         const uint64_t stride = (uint64_t)tm.ctas * blockDim.x;
         const uint64_t tid = (uint64_t)rank * blockDim.x + threadIdx.x;
-        if (d.touched) {
-            const uint64_t cnt = ld_vol64(d.touched_count);
+        // Where either clear will do, scattered stores costing about a
+        // 32-byte sector each against streaming ones, the list is used while
+        // it covers under a quarter of the table's words.
+        const uint64_t cnt = d.touched ? ld_vol64(d.touched_count) : 0;
+        if (d.touched && cnt <= d.touched_cap &&
+            (!d.clear_either || cnt * d.prev_slot_words * 4 < d.table_words)) {
             for (uint64_t i = tid; i < cnt; i += stride) {
                 const uint32_t w = __ldcg(d.touched + i);
                 if (w == kTouchedHole) continue;

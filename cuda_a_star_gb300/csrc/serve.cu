@@ -95,7 +95,8 @@ struct gastar_server {
     gastar_ctx* ctx = nullptr;
     gastar_serve_config cfg;
     DevBuf arena, descs, ctls, order, counters, path_descs, path_arena, team_ctl, team_stage;
-    uint32_t heavy_teams = 0;
+    uint32_t heavy_teams = 0;   // team buffers allocated (the most teams a launch can hold)
+    uint32_t resident = 0;      // blocks resident on the device at once
     uint64_t heavy_stage_bytes = 0;
     uint32_t heap_snodes = kHeapSmemNodes;  // shared-memory heap nodes per warp
     RangeAlloc alloc;
@@ -259,11 +260,14 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
     s->heap_snodes = fit_heap_snodes(c, kKindsAll, cf.warps_per_block, cf.expansion_width, false, s->threads, nb,
                                      &s->smem, buckets);
     const uint32_t resident = (uint32_t)(nb * c->sms);
+    s->resident = resident;
     s->max_active = cf.max_active ? cf.max_active : resident;
     const uint32_t m = s->max_active;
     if (!cf.heavy_team) cf.heavy_team = 1;
     if (cf.heavy_team > 1) {
-        s->heavy_teams = cf.heavy_teams ? cf.heavy_teams : std::max(1u, resident / 4 / cf.heavy_team);
+        // Buffers for as many teams as the resident blocks hold; each step
+        // uses as many as its heavy requests and the light ones leave room for.
+        s->heavy_teams = cf.heavy_teams ? cf.heavy_teams : resident / cf.heavy_team;
         s->heavy_teams = std::min(s->heavy_teams, resident / cf.heavy_team);
         s->heavy_stage_bytes = team_stage_bytes(cf.heavy_team, cf.warps_per_block, cf.expansion_width, 8, 16);
         if (!s->heavy_teams || !s->team_ctl.ensure(sizeof(TeamCtl) * s->heavy_teams) ||
@@ -366,7 +370,16 @@ int gastar_serve_step(gastar_server* s) {
     P.barrier_timeout_ns = 2000000000ull;
     uint32_t blocks = std::min((uint32_t)light.size(), s->max_active);
     if (!heavy.empty()) {
-        const uint32_t teams = std::min<uint32_t>(s->heavy_teams, (uint32_t)heavy.size());
+        // One-block requests keep up to a quarter of the resident blocks (as
+        // many as there are of them); heavy requests get the rest in teams.
+        // Team blocks that run out of heavy requests take one-block requests,
+        // and every block of the launch is resident (a cooperative launch),
+        // so a team's blocks always run together.
+        const uint32_t T = s->cfg.heavy_team;
+        const uint32_t reserve = std::min<uint32_t>((uint32_t)light.size(), s->resident / 4);
+        uint32_t teams = std::max(1u, (s->resident - reserve) / T);
+        teams = std::min({teams, s->heavy_teams, (uint32_t)heavy.size()});
+        blocks = std::min(s->resident, teams * T + (uint32_t)light.size());
         P.heavy_order = reinterpret_cast<const uint32_t*>(s->order.p) + light.size();
         P.n_heavy = (uint32_t)heavy.size();
         P.heavy_team = s->cfg.heavy_team;
@@ -375,7 +388,6 @@ int gastar_serve_step(gastar_server* s) {
         P.heavy_ctl = reinterpret_cast<TeamCtl*>(s->team_ctl.p);
         P.heavy_stage = s->team_stage.p;
         P.heavy_stage_bytes = s->heavy_stage_bytes;
-        blocks = std::max(blocks, teams * s->cfg.heavy_team);
         if (!cuda_ok(cudaMemsetAsync(s->team_ctl.p, 0, sizeof(TeamCtl) * teams, st), "cudaMemsetAsync"))
             return GASTAR_CUDA_ERROR;
     }

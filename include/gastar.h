@@ -236,7 +236,9 @@ typedef struct gastar_serve_config {
     uint32_t delta_grid;       /* pop window for grid requests (0 = none) */
     uint64_t sliding_states;   /* expected max states per puzzle request (0 = by size) */
     uint32_t heavy_team;       /* blocks per team for heavy requests (1 = no teams) */
-    uint32_t heavy_teams;      /* teams per launch (0 = a quarter of the resident blocks) */
+    uint32_t heavy_teams;      /* most teams per launch (0 = as many as the resident blocks
+                                  hold); each launch leaves up to a quarter of the resident
+                                  blocks to the one-block requests it has */
     uint64_t heavy_cells;      /* grids with at least this many cells are heavy */
     uint32_t open_list;        /* 0 = warp-heaps; 1 (default) = f-buckets (pages in the
                                   partition, state kept there between steps) in front of
@@ -271,6 +273,15 @@ int gastar_serve_stats(gastar_server *srv, uint32_t *waiting, uint32_t *active,
  * *gbs = sectors x 32 bytes / kernel time; *ms = that kernel time. */
 int gastar_measure_random_peak(gastar_ctx *ctx, uint64_t buffer_bytes, uint32_t kind, double *gbs,
                                double *ms);
+/* The same measurement with its shape as arguments, for sweeping the
+ * denominator (no reference counterpart): the buffer is the largest power of
+ * two <= buffer_bytes (at least 1 MiB, so L2-resident sizes are allowed);
+ * in_flight = independent accesses each thread keeps outstanding (1, 2, 4, 8,
+ * 16 or 32); loads_per_sector = 16-byte loads per 32-byte sector for kind 0
+ * (1 or 2; either moves the whole sector).  GASTAR_BAD_INPUT otherwise. */
+int gastar_measure_random_peak_ex(gastar_ctx *ctx, uint64_t buffer_bytes, uint32_t kind,
+                                  uint32_t in_flight, uint32_t loads_per_sector, double *gbs,
+                                  double *ms);
 
 /* ---- text formats and synthetic instances (host only, no GPU needed) ---- */
 /* Reads "start goal" in the reference's sliding format (Position(std::istream&),

@@ -127,3 +127,46 @@ def test_heavy_teams_and_promotion(engine, oracle, gastar):
     for kind, a, idx, side in cases:
         assert b.result(idx, path=False).status_name == "OK"
     b.close()
+
+
+def test_config_b_shape_against_oracle(engine, oracle, gastar):
+    """A stratified sample of the 1024-instance batched mix at its own sizes:
+    15-puzzles with walks 20-80 (the hard ones pass the promotion budget and
+    are re-solved by the plain engine) and grids of side 256-2048 with obstacle
+    density 0.1-0.3 (the largest on two-block teams), under the autotuner's
+    usual pick.  Every cost equals the oracle's and every path is valid, on
+    the first run and on two device-resident re-runs, which clear only the
+    table slots the previous search claimed."""
+    seed0 = 0x3_0000  # the batched mix of the benchmark
+    rng = np.random.default_rng(seed0)
+    sides, dens = [], []
+    for _ in range(512):  # the benchmark's draw order: side, then density, per grid
+        sides.append(int(rng.integers(256, 2049)))
+        dens.append(float(rng.uniform(0.1, 0.3)))
+    b = engine.batch(warps_per_block=16, expansion_width=32, load_factor=0.5, delta_grid=18,
+                     heavy_team=2, heavy_cells=1 << 21, open_list=1)
+    puzzles = [gastar.gen_sliding(4, seed0 + i, 20, 80) for i in range(0, 512, 8)]
+    order = sorted(range(512), key=lambda i: sides[i])
+    picks = order[::32] + order[-2:]  # sides across the range, the two largest included
+    grids = [(gastar.gen_grid(sides[i], sides[i], seed0 + 100_000 + i, dens[i]), sides[i]) for i in picks]
+    for s, g in puzzles:
+        b.add_sliding(s, g)
+    for w, side in grids:
+        b.add_grid(w, (0, 0), (side - 1, side - 1))
+    _, ref_p = oracle.sliding_batch(4, np.stack([s for s, _ in puzzles]), np.stack([g for _, g in puzzles]))
+    _, ref_g = oracle.grid_batch([(w, (0, 0), (side - 1, side - 1)) for w, side in grids])
+    want = [r.cost for r in ref_p] + [r.cost for r in ref_g]
+    b.run()
+    assert b.stats()["promoted"] > 0  # the plain-engine re-solve path ran
+    for run in range(3):
+        if run:
+            b.rerun()
+        res = [b.result(i, path=True) for i in range(len(b))]
+        assert [r.status_name for r in res] == ["OK"] * len(res)
+        assert [r.cost for r in res] == want, run
+        for i, (s, g) in enumerate(puzzles):
+            assert oracle.sliding_validate(4, s, g, res[i].path) == (True, want[i])
+        for j, (w, side) in enumerate(grids):
+            k = len(puzzles) + j
+            assert oracle.grid_validate(w, (0, 0), (side - 1, side - 1), res[k].path) == (True, want[k])
+    b.close()
