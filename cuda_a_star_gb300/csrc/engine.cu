@@ -381,7 +381,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     uint64_t heaps = (Q + ew - 1) / ew;
     // Warps per block 0 = 8 when that still gives at least half of the SMs a
     // block (fewer, larger blocks: fewer parties to the hand-offs), else 4.
-    const uint32_t W = cfg.warps_per_block ? std::min(8u, cfg.warps_per_block)
+    const uint32_t W = cfg.warps_per_block ? std::min(16u, cfg.warps_per_block)
                                            : ((heaps / 8 >= (uint64_t)c->sms / 2) ? 8u : 4u);
     const uint32_t threads = W * 32;
     uint64_t blocks = (heaps + W - 1) / W;

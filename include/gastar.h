@@ -59,8 +59,10 @@ typedef struct gastar_config {
     uint32_t moves;            /* gastar_moves (sliding puzzles only) */
     uint32_t expansion_width;  /* entries each warp-heap pops per iteration, 1..32;
                                   0 = auto, clamp(num_queues / 1024, 8, 32) */
-    uint32_t warps_per_block;  /* warp-heaps per thread block, 1..8; 0 = auto (8 when the
-                                  blocks still cover half of the SMs, else 4) */
+    uint32_t warps_per_block;  /* warp-heaps per thread block, 1..16 (above 8: the
+                                  512-thread kernel, at most 128 registers per thread);
+                                  0 = auto (8 when the blocks still cover half of the
+                                  SMs, else 4) */
     uint32_t max_blocks;       /* cap on thread blocks for one instance (0 = all SMs) */
     float load_factor;         /* table load limit before GASTAR_TABLE_FULL (0.5..0.9) */
     uint32_t table_log2;       /* hash-table slots = 2^table_log2 (0 = adaptive) */
