@@ -413,7 +413,7 @@ def run_batched(g, eng, steps: int, check: bool = True) -> dict:
                                     "delta_grid", "heavy_team", "heavy_cells", "open_list")}
     # end to end: host buffers -> upload -> solve -> results and paths back;
     # the median of three runs (one run is exposed to host-side noise)
-    e2e_runs = []
+    e2e_runs, e2e_kernel_ms = [], []
     for rep in range(3):
         if rep:
             b.close()
@@ -423,6 +423,7 @@ def run_batched(g, eng, steps: int, check: bool = True) -> dict:
         b.run()
         res_paths = [b.result(i, path=True) for i in range(len(b))]
         e2e_runs.append(time.perf_counter() - t0)
+        e2e_kernel_ms.append(b.stats()["kernel_ms"])
     e2e_s = statistics.median(e2e_runs)
     st0 = b.stats()
     # device-resident reruns (graph replay)
@@ -463,6 +464,7 @@ def run_batched(g, eng, steps: int, check: bool = True) -> dict:
         "e2e": {"value": n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": st0["h2d_bytes"],
                 "d2h_bytes_per_step": st0["d2h_bytes"],
                 "runs_s": [round(x, 4) for x in e2e_runs],
+                "runs_kernel_ms": [round(x, 1) for x in e2e_kernel_ms],
                 "how": "gastar_batch_create/add/run/result with host buffers, paths copied back; "
                        "median of 3"},
         "device_bytes": st0["device_bytes"],

@@ -126,7 +126,7 @@ uint32_t fit_heap_snodes(gastar_ctx* c, uint32_t kinds, uint32_t warps, uint32_t
 int occupancy_blocks(gastar_ctx* /*c: the current device's context*/, uint32_t kinds, uint32_t threads,
                      size_t smem) {
     const void* f = search_kernel_for(kinds, threads);
-    if (smem > 48 * 1024)
+    if (smem > kSmemNoOptIn)
         if (!cuda_ok(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                      "cudaFuncSetAttribute"))
             return 0;
@@ -140,7 +140,7 @@ int occupancy_blocks(gastar_ctx* /*c: the current device's context*/, uint32_t k
 int launch_search(gastar_ctx* /*c: the current device's context*/, uint32_t kinds, const LaunchParams& P,
                   uint32_t blocks, uint32_t threads, size_t smem, cudaStream_t st) {
     const void* f = search_kernel_for(kinds, threads);
-    if (smem > 48 * 1024)
+    if (smem > kSmemNoOptIn)
         GA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     LaunchParams p = P;
     void* args[] = {&p};

@@ -53,6 +53,10 @@ constexpr uint32_t kTouchedHole = 0xffffffffu;
 
 // Warp-heap nodes below sn live in shared memory (node 0 in registers).
 constexpr uint32_t kHeapSmemNodes = 7;      // default sn: nodes 1..6
+// Dynamic shared memory above this needs the opt-in attribute: a block's
+// static shared memory (the kernels' CtaShared, ~1.2 KB) counts against the
+// default 48 KiB as well.
+constexpr size_t kSmemNoOptIn = 44 * 1024;
 constexpr uint32_t kHeapSmemNodesMax = 127;  // levels 0..6
 // Global stage area of a multi-block team: kStageRing buffers, each one
 // region of warps*ew*maxn entries per block; then one 64-bit ready word per

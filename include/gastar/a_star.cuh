@@ -86,7 +86,7 @@ std::pair<std::vector<T>, std::chrono::nanoseconds> solve(const T& start, const 
     const size_t smem = (multi ? 0 : 2 * stage_entries_per_buffer(W, ew, D::MAXN) * sizeof(E)) +
                         (size_t)W * (kHeapSmemNodes - 1) * 32 * sizeof(E);
     const void* kern = reinterpret_cast<const void*>(&plugin_search_kernel<D>);
-    if (smem > 48 * 1024)
+    if (smem > kSmemNoOptIn)
         check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
               "cudaFuncSetAttribute");
     int nb = 0;
