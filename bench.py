@@ -592,6 +592,8 @@ def run_served(g, eng, check: bool = True) -> dict:
                "latency_ms_by_class": {
                    c: {"p50": _pct(lat[k::4], 0.5), "p99": _pct(lat[k::4], 0.99),
                        "max": max(lat[k::4])} for k, c in enumerate(SERVED_CLASSES)},
+               "expansions_by_class": {c: sum(res[j].expansions for j in range(k, len(reqs), 4))
+                                       for k, c in enumerate(SERVED_CLASSES)},
                "solved": sum(1 for r in res.values() if r.status == g.OK)}
         return out, res
 

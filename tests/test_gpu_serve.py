@@ -76,3 +76,34 @@ def test_budget_limits_admission(engine, oracle, gastar):
     for r, i in zip(reqs, ids):
         _check(oracle, r, out[i])
     srv.close()
+
+
+def test_served_mix_at_benchmark_sizes(engine, oracle, gastar):
+    """Requests at the served benchmark's own sizes -- 8-puzzles (walk 60),
+    15-puzzles (walk 20-80), 24-puzzles (walk 20-40, 128-bit keys) and grids
+    of side 512-5000 (the larger ones heavy, on multi-block teams) -- arriving
+    while the server runs under its default configuration: every cost equals
+    the oracle's and every path is valid."""
+    reqs = [("s", *gastar.gen_sliding(3, 6000 + i, 60, 60)) for i in range(4)]
+    reqs += [("s", *gastar.gen_sliding(4, 6100 + i, 20, 80)) for i in range(6)]
+    reqs += [("s", *gastar.gen_sliding(5, 6200 + i, 20, 40)) for i in range(4)]
+    for i, side in enumerate((512, 1500, 3000, 5000)):
+        reqs.append(("g", gastar.gen_grid(side, side, 6300 + i, 0.2), (0, 0), (side - 1, side - 1)))
+    order = np.random.default_rng(6400).permutation(len(reqs))
+    srv = engine.server(budget_bytes=64 << 30)
+    ids = {}
+    for k, j in enumerate(order):
+        ids[int(j)] = _submit(srv, reqs[j])
+        if k % 3 == 2:
+            srv.step()
+    out = srv.drain(list(ids.values()))
+    srv.close()
+    gi = [j for j, r in enumerate(reqs) if r[0] == "g"]
+    _, ref_g = oracle.grid_batch([reqs[j][1:] for j in gi])
+    for j, o in zip(gi, ref_g):
+        r, res = reqs[j], out[ids[j]]
+        assert res.status_name == "OK" and res.cost == o.cost
+        assert oracle.grid_validate(r[1], r[2], r[3], res.path) == (True, res.cost)
+    for j, r in enumerate(reqs):
+        if r[0] == "s":
+            _check(oracle, r, out[ids[j]])
