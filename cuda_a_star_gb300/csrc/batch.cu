@@ -136,7 +136,7 @@ void gastar_batch_config_default(gastar_batch_config* cfg) {
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
     cfg->use_graph = 1;
-    cfg->delta_grid = 18;
+    cfg->delta_grid = 12;
     cfg->heavy_team = 2;
     cfg->heavy_cells = 1ull << 21;
     cfg->promote_expansions = 1ull << 21;
@@ -865,7 +865,7 @@ extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const cha
                          {16, 32})) != GASTAR_OK)
         return rc;
     if (grids && (rc = try_values([](gastar_batch_config& c, double v) { c.delta_grid = (uint32_t)v; },
-                                  {18, 36, 72})) != GASTAR_OK)
+                                  {9, 12, 18, 36})) != GASTAR_OK)
         return rc;
     if (heavy && (rc = try_values([](gastar_batch_config& c, double v) { c.heavy_team = (uint32_t)v; },
                                   {1, 2, 4, 8})) != GASTAR_OK)
