@@ -230,17 +230,23 @@ def _mixed_instances(g):
     return p15, grids
 
 
+# Pop window of the plain engine's grid solves (one grid over the whole GPU,
+# bound by iteration latency): wider windows mean fewer iterations; on the
+# 4096^2 and 8192^2 grids the time falls up to 54 and is flat from 54 to 144.
+GRID_DELTA_PLAIN = 72
+
+
 def run_grid4k(g, eng, check: bool) -> dict:
     """Plain GA* on the 4096 x 4096 weighted grid (weights 1..9, 20 %
     obstacles, monotone corridor (0,0) -> (4095,4095)): device time of the
     solve, expansions/s, and its cost against the CPU oracle."""
     wts = g.gen_grid(4096, 4096, 0x4096, 0.2)
-    cfg = g.make_config(num_queues=16384, delta=36)
+    cfg = g.make_config(num_queues=16384, delta=GRID_DELTA_PLAIN)
     eng.solve_grid(wts, (0, 0), (4095, 4095), config=cfg)  # warm-up
     runs = [eng.solve_grid(wts, (0, 0), (4095, 4095), config=cfg) for _ in range(3)]
     r = min(runs, key=lambda x: x.kernel_ms)
     out = {"workload": "plain GA*, 4096x4096 grid, weights 1-9, 20% obstacles, corridor; Q=16384, "
-                       "pop window 36",
+                       f"pop window {GRID_DELTA_PLAIN}",
            "kernel_ms": r.kernel_ms, "total_ms": r.total_ms, "cost": r.cost,
            "node_expansions_per_s": r.expansions / (r.kernel_ms / 1000.0)}
     if check:
@@ -448,7 +454,8 @@ def run_batched(g, eng, steps: int, check: bool = True) -> dict:
             r = eng.solve_sliding(*p15[i], 4, num_queues=16384, path=True, path_cap=1024)
         else:
             w, side = grids[i - len(p15)]
-            r = eng.solve_grid(w, (0, 0), (side - 1, side - 1), num_queues=16384, delta=36, path=True)
+            r = eng.solve_grid(w, (0, 0), (side - 1, side - 1), num_queues=16384, delta=GRID_DELTA_PLAIN,
+                               path=True)
         t_plain += r.total_ms / 1000.0
     plain_sps = len(sample) / t_plain
     peak, peak_kind = _peaks()
@@ -617,7 +624,7 @@ def run_served(g, eng, check: bool = True) -> dict:
         if r[0] == "s":
             x = eng.solve_sliding(r[1], r[2], path=True, path_cap=1024)
         else:
-            x = eng.solve_grid(r[1], r[2], r[3], num_queues=16384, delta=36, path=True)
+            x = eng.solve_grid(r[1], r[2], r[3], num_queues=16384, delta=GRID_DELTA_PLAIN, path=True)
         t_plain += x.total_ms / 1000.0
     plain_sps = len(sample) / t_plain
     out = {"workload": SERVED["name"], "requests": len(reqs), "capacity_solves_per_s": cap,
