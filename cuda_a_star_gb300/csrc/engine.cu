@@ -386,6 +386,14 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     const uint32_t threads = W * 32;
     uint64_t blocks = (heaps + W - 1) / W;
     const bool multi = blocks > 1;
+    // Widening: a puzzle search with the automatic width that passes
+    // kWideAfter iterations is a hard one, whose iteration count the pops per
+    // iteration set rather than its depth; from then on every warp-heap pops
+    // twice as many (at most 32).  On the 64 15-puzzles of the plain
+    // benchmark (Q = 16384) the four hardest took 150-359 iterations and ran
+    // 1.3-1.4x faster with twice the pops, the rest at most ~90 iterations.
+    const uint32_t ew_wide =
+        multi && pp.kind != KIND_GRID && !cfg.expansion_width ? std::min(32u, 2 * ew) : ew;
     size_t smem = block_smem_bytes(kinds, W, ew, multi);
     const int nb = occupancy_blocks(c, kinds, threads, smem);
     if (nb <= 0) return GASTAR_CUDA_ERROR;
@@ -424,7 +432,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
         limit = (uint64_t)((double)slots * lf);
         // Claims stop within two iterations past the limit; every warp may
         // leave one chunk partly unused.
-        touched_cap = limit + 2 * heaps * ew * maxn + heaps * kTouchedChunk + 16;
+        touched_cap = limit + 2 * heaps * ew_wide * maxn + heaps * kTouchedChunk + 16;
         tb = &c->table;
         // A reallocated table, claim list or claim counter loses the record of
         // what the previous solve wrote: clear the whole table then.
@@ -447,7 +455,7 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     uint64_t cap_nodes = std::max<uint64_t>(2 * snodes, (per_heap * 2 + 31) / 32);
     if (cap_nodes > 0x7fffffffull) return GASTAR_OUT_OF_MEMORY;
     const size_t heap_bytes = (size_t)heaps * (cap_nodes + 1) * 32 * ebytes;
-    const size_t stage_bytes = multi ? team_stage_bytes((uint32_t)blocks, W, ew, maxn, ebytes) : 16;
+    const size_t stage_bytes = multi ? team_stage_bytes((uint32_t)blocks, W, ew_wide, maxn, ebytes) : 16;
 
     if (!c->heaps.ensure(heap_bytes) || !c->hdr.ensure((size_t)heaps * 8) ||
         !c->stage.ensure(stage_bytes) || !c->launch.ensure(kLbBytes))
@@ -482,6 +490,10 @@ static int plain_attempt(gastar_ctx* c, const PlainProblem& pp, const gastar_con
     d.heap_hdr = reinterpret_cast<uint32_t*>(c->hdr.p);
     d.heap_cap = (uint32_t)cap_nodes;
     d.ew = ew;
+    if (ew_wide > ew) {
+        d.ew_wide = ew_wide;
+        d.wide_after = kWideAfter;
+    }
     d.max_exp = cfg.max_expansions;
     d.timeout_ns = (uint64_t)cfg.timeout_ms * 1000000ull;
     d.max_iter = cfg.max_iterations;

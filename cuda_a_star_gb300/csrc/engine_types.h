@@ -46,6 +46,10 @@ static_assert(kStageRing >= kCutLag + 2, "a stage buffer must be consumed before
 
 constexpr uint32_t kSlotsHost = 4;
 
+// Plain engine: iteration from which a puzzle search with the automatic
+// expansion width pops twice as many entries per warp-heap.
+constexpr uint32_t kWideAfter = 64;
+
 // Claim list: each warp reserves this many entries at a time; entries a warp
 // reserved but did not use hold kTouchedHole.
 constexpr uint32_t kTouchedChunk = 1024;
@@ -117,7 +121,12 @@ struct alignas(16) InstDesc {
     // (heaps * bq_pages words), then their free-page stacks (as many words),
     // then each heap's saved bucket state (kBucketStateWords words).
     void* bq_base;
-    uint32_t bq_pages, pad2;
+    uint32_t bq_pages;
+    // Widening (multi-block teams): from iteration wide_after on (0 = never)
+    // each warp-heap pops up to ew_wide entries instead of ew; the stage
+    // regions are sized for ew_wide.
+    uint32_t ew_wide;
+    uint32_t wide_after, pad2;
 };
 
 constexpr uint32_t kBucketStateWords = 128;

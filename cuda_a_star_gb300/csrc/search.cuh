@@ -503,7 +503,8 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     const uint32_t rank = tm.rank;
     const uint32_t H = d.heaps;
     TeamSlot* slots = sm.slot;  // one-block teams
-    const size_t stage_cap = stage_entries_per_buffer(H, d.ew, MAXN);
+    const uint32_t ew_cap = d.ew_wide > d.ew ? d.ew_wide : d.ew;  // widest pop of the search
+    const size_t stage_cap = stage_entries_per_buffer(H, ew_cap, MAXN);
     char* dyn = reinterpret_cast<char*>(g_dyn_smem);
     E* const stage0 = multi ? reinterpret_cast<E*>(tm.stage) : reinterpret_cast<E*>(dyn);  // ring (multi)
     E* const snodes_all = reinterpret_cast<E*>(dyn + (multi ? 0 : 2 * stage_cap * sizeof(E)));
@@ -613,7 +614,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
     // Multi-block teams: each block stages into its own region of the ring
     // buffers and aggregates its counters and minima in shared memory; thread
     // 0 publishes them (ready word, cut slot).
-    const size_t region_cap = stage_entries_per_buffer(W, d.ew, MAXN);
+    const size_t region_cap = stage_entries_per_buffer(W, ew_cap, MAXN);
     unsigned long long* const ready =
         multi ? reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(tm.stage) +
                                                       (size_t)kStageRing * stage_cap * sizeof(E))
@@ -690,7 +691,8 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
                                  ? ((uint64_t)(fmin + d.delta + 1) << 32)
                                  : kInfPrio;
         E e;
-        const uint32_t cnt = open_pop(hp, bq, ew, lim, e, lane);
+        const uint32_t cnt =
+            open_pop(hp, bq, d.wide_after && it0 + it >= d.wide_after ? d.ew_wide : ew, lim, e, lane);
         bool act = (uint32_t)lane < cnt;
         const KeyT k = D::key_of(e);
         const uint32_t g = prio_g(e.prio), h = prio_f(e.prio) - g;

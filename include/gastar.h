@@ -58,7 +58,9 @@ typedef struct gastar_config {
     uint32_t heuristic;        /* gastar_heuristic */
     uint32_t moves;            /* gastar_moves (sliding puzzles only) */
     uint32_t expansion_width;  /* entries each warp-heap pops per iteration, 1..32;
-                                  0 = auto, clamp(num_queues / 1024, 8, 32) */
+                                  0 = auto, clamp(num_queues / 1024, 8, 32), and a
+                                  puzzle search on several blocks that passes 64
+                                  iterations then pops twice as many (at most 32) */
     uint32_t warps_per_block;  /* warp-heaps per thread block, 1..16 (above 8: the
                                   512-thread kernel, at most 128 registers per thread);
                                   0 = auto (8 when the blocks still cover half of the
