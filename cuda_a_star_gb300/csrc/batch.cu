@@ -136,7 +136,7 @@ void gastar_batch_config_default(gastar_batch_config* cfg) {
     cfg->heuristic = GASTAR_H_ADMISSIBLE;
     cfg->moves = GASTAR_MOVES_STANDARD;
     cfg->use_graph = 1;
-    cfg->delta_grid = 12;
+    cfg->delta_grid = 9;
     cfg->heavy_team = 2;
     cfg->heavy_cells = 1ull << 21;
     cfg->promote_expansions = 1ull << 21;
@@ -878,6 +878,12 @@ extern "C" int gastar_batch_autotune(gastar_batch* b, uint32_t sample, const cha
     if (heavy && best.heavy_team > 1 &&
         (rc = try_values([](gastar_batch_config& c, double v) { c.heavy_cells = (uint64_t)v; },
                          {(double)(1u << 20), (double)(1u << 21), (double)(1u << 22)})) != GASTAR_OK)
+        return rc;
+    // The pop window again under the chosen teams: with two-block teams on the
+    // batched mix windows 9 and 12 tie, with one-block grids 9 is ~10 % faster.
+    if (grids && heavy &&
+        (rc = try_values([](gastar_batch_config& c, double v) { c.delta_grid = (uint32_t)v; },
+                         {9, 12, 18})) != GASTAR_OK)
         return rc;
     if ((rc = try_values([](gastar_batch_config& c, double v) { c.load_factor = (float)v; },
                          {0.5, 0.7, 0.85})) != GASTAR_OK)
