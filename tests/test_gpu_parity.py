@@ -179,3 +179,20 @@ def test_4096_grid_full_size(engine, oracle, gastar, delta):
     r = engine.solve_grid(wts, (0, 0), (4095, 4095), num_queues=16384, delta=delta)
     _check_grid(oracle, wts, (0, 0), (4095, 4095), r)
     assert len(r.path) > 4095 and r.path[0] == 0 and r.path[-1] == 4096 * 4096 - 1
+
+
+def test_widened_pops_on_the_hardest_benchmark_puzzles(engine, oracle, gastar):
+    """The plain benchmark's three hardest 15-puzzles (seeds 0x150000 + 38,
+    17, 31 of its walk 40-80 set) run for hundreds of iterations at Q = 16384:
+    past the 64th the automatic width doubles every warp-heap's pops.  Costs
+    equal the oracle's and paths are valid, widened and at a fixed width."""
+    insts = [gastar.gen_sliding(4, 0x15_0000 + i, 40, 80) for i in (38, 17, 31)]
+    _, ref = oracle.sliding_batch(4, np.stack([s for s, _ in insts]), np.stack([g for _, g in insts]))
+    for (s, g), o in zip(insts, ref):
+        wide = engine.solve_sliding(s, g, 4, num_queues=16384, table_log2=30)
+        assert wide.iterations > 64  # the widened iterations ran
+        fixed = engine.solve_sliding(s, g, 4, num_queues=16384, table_log2=30, expansion_width=16)
+        for r in (wide, fixed):
+            assert r.status_name == "OK" and r.cost == o.cost
+            assert oracle.sliding_validate(4, s, g, r.path) == (True, r.cost)
+        assert wide.iterations < fixed.iterations
