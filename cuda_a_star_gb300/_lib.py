@@ -71,7 +71,7 @@ class ServeConfig(C.Structure):
         ("load_factor", C.c_float), ("heuristic", C.c_uint32), ("moves", C.c_uint32),
         ("delta_grid", C.c_uint32), ("sliding_states", C.c_uint64),
         ("heavy_team", C.c_uint32), ("heavy_teams", C.c_uint32), ("heavy_cells", C.c_uint64),
-        ("open_list", C.c_uint32), ("pad", C.c_uint32),
+        ("open_list", C.c_uint32), ("promote_log2", C.c_uint32),
     ]
 
 

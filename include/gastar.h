@@ -247,7 +247,10 @@ typedef struct gastar_serve_config {
     uint32_t open_list;        /* 0 = warp-heaps; 1 (default) = f-buckets (pages in the
                                   partition, state kept there between steps) in front of
                                   the warp-heaps */
-    uint32_t pad;
+    uint32_t promote_log2;     /* a 15- or 24-puzzle request past 2^promote_log2
+                                  expansions leaves its slot and is finished by the plain
+                                  engine on the whole GPU between two steps (0 = never;
+                                  default 18) */
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);

@@ -107,3 +107,22 @@ def test_served_mix_at_benchmark_sizes(engine, oracle, gastar):
     for j, r in enumerate(reqs):
         if r[0] == "s":
             _check(oracle, r, out[ids[j]])
+
+
+def test_hard_puzzles_promoted_to_the_plain_engine(engine, oracle, gastar):
+    """With a low promotion budget (2^12 expansions) most 15- and 24-puzzle
+    requests leave their slot mid-search and are finished by the plain engine
+    between two steps; grids and 8-puzzles stay; every result matches the
+    oracle, paths included."""
+    reqs = [("s", *gastar.gen_sliding(4, 6500 + i, 30, 60)) for i in range(6)]
+    reqs += [("s", *gastar.gen_sliding(5, 6600 + i, 16, 24)) for i in range(2)]
+    reqs += [("s", *gastar.gen_sliding(3, 6700 + i, 60, 60)) for i in range(2)]
+    reqs.append(("g", gastar.gen_grid(300, 280, 6800, 0.2), (0, 0), (299, 279)))
+    srv = engine.server(slice_iters=16, budget_bytes=8 << 30, promote_log2=12)
+    ids = [_submit(srv, r) for r in reqs]
+    out = srv.drain(ids)
+    srv.close()
+    for r, i in zip(reqs, ids):
+        _check(oracle, r, out[i])
+    # at least the 15-puzzles passed 2^12 expansions (and were promoted)
+    assert sum(out[i].expansions > (1 << 12) for i in ids[:6]) >= 3
