@@ -17,7 +17,7 @@ EXPORTS = [
     "gastar_config_default", "gastar_create", "gastar_destroy", "gastar_last_error",
     "gastar_status_name", "gastar_version", "gastar_device_info",
     "gastar_solve_sliding", "gastar_solve_grid", "gastar_solve_grid_device",
-    "gastar_solve_sliding_noalloc",
+    "gastar_solve_sliding_noalloc", "gastar_grid_min_weight",
     "gastar_batch_config_default", "gastar_batch_create", "gastar_batch_destroy",
     "gastar_batch_add_sliding", "gastar_batch_add_grid", "gastar_batch_run",
     "gastar_batch_rerun", "gastar_batch_count", "gastar_batch_result", "gastar_batch_path",
@@ -72,6 +72,7 @@ class ServeConfig(C.Structure):
         ("delta_grid", C.c_uint32), ("sliding_states", C.c_uint64),
         ("heavy_team", C.c_uint32), ("heavy_teams", C.c_uint32), ("heavy_cells", C.c_uint64),
         ("open_list", C.c_uint32), ("promote_log2", C.c_uint32),
+        ("admit_bypass", C.c_uint32), ("weights_pool", C.c_uint32),
     ]
 
 
@@ -110,6 +111,7 @@ def load(path: str | None = None) -> C.CDLL:
                                                C.c_uint32, C.c_uint32, C.c_uint32,
                                                C.POINTER(Config), u32p, C.c_uint32,
                                                C.POINTER(Result)]),
+        "gastar_grid_min_weight": (C.c_int, [vp, C.c_uint32, C.c_uint32, u8p, u32p, C.POINTER(C.c_int)]),
         "gastar_batch_config_default": (None, [C.POINTER(BatchConfig)]),
         "gastar_batch_create": (vp, [vp, C.POINTER(BatchConfig)]),
         "gastar_batch_destroy": (None, [vp]),

@@ -54,6 +54,64 @@ int device_min_weight(gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStr
     return GASTAR_OK;
 }
 
+// Copies a grid from host memory that the GPU reads in place (pageable
+// memory through the host's page tables) and reduces its least passable
+// weight in the same pass: per byte, min(w - 1) with 0 (obstacle) wrapping to
+// 0xff, 16 bytes per load where both pointers allow it.
+__global__ void copy_min_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, uint64_t cells,
+                                uint32_t* out) {
+    uint32_t m = 0xffffffffu;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nth = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t done = 0;
+    if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+        const uint64_t n16 = cells / 16;
+        const uint4* s = reinterpret_cast<const uint4*>(src);
+        uint4* d = reinterpret_cast<uint4*>(dst);
+        for (uint64_t i = tid; i < n16; i += nth) {
+            const uint4 v = s[i];
+            d[i] = v;
+            m = __vminu4(m, __vsub4(v.x, 0x01010101u));
+            m = __vminu4(m, __vsub4(v.y, 0x01010101u));
+            m = __vminu4(m, __vsub4(v.z, 0x01010101u));
+            m = __vminu4(m, __vsub4(v.w, 0x01010101u));
+        }
+        done = n16 * 16;
+    }
+    for (uint64_t i = done + tid; i < cells; i += nth) {
+        const uint32_t b = src[i];
+        dst[i] = (uint8_t)b;
+        m = __vminu4(m, ((b - 1u) & 0xffu) | 0xffffff00u);
+    }
+    uint32_t r = min(min(m & 0xffu, (m >> 8) & 0xffu), min((m >> 16) & 0xffu, m >> 24));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = min(r, __shfl_xor_sync(kFull, r, o));
+    if ((threadIdx.x & 31) == 0 && r != 0xffu) atomicMin(out, r);
+}
+
+int upload_grid(gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint64_t cells, cudaStream_t st,
+                uint32_t* minw) {
+    if (!c->host_direct) {
+        if (!cuda_ok(cudaMemcpyAsync(d_dst, h_src, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+            return GASTAR_CUDA_ERROR;
+        return device_min_weight(c, d_dst, cells, st, minw);
+    }
+    if (!c->misc.ensure(64)) return GASTAR_OUT_OF_MEMORY;
+    uint32_t* d = reinterpret_cast<uint32_t*>(c->misc.p) + 9;
+    const uint32_t init = 0xffu;
+    if (!cuda_ok(cudaMemcpyAsync(d, &init, 4, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
+        return GASTAR_CUDA_ERROR;
+    const uint64_t blocks = std::min<uint64_t>((cells / 16 + 255) / 256, (uint64_t)c->sms * 8);
+    copy_min_kernel<<<(unsigned)std::max<uint64_t>(1, blocks), 256, 0, st>>>(h_src, d_dst, cells, d);
+    if (!cuda_ok(cudaGetLastError(), "copy_min_kernel")) return GASTAR_CUDA_ERROR;
+    uint32_t r = 0xffu;
+    if (!cuda_ok(cudaMemcpyAsync(&r, d, 4, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync") ||
+        !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+        return GASTAR_CUDA_ERROR;
+    *minw = r == 0xffu ? 255u : r + 1u;
+    return GASTAR_OK;
+}
+
 }  // namespace gastar
 
 using namespace gastar;
@@ -213,10 +271,8 @@ int gastar_batch_add_grid(gastar_batch* b, uint32_t w, uint32_t h, const uint8_t
         return -GASTAR_OUT_OF_MEMORY;
     }
     cudaStream_t st = b->ctx->stream;
-    if (!cuda_ok(cudaMemcpyAsync(d, weights, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
-        return -GASTAR_CUDA_ERROR;
     uint32_t mw = 255;
-    const int rc = device_min_weight(b->ctx, d, cells, st, &mw);
+    const int rc = upload_grid(b->ctx, d, weights, cells, st, &mw);
     if (rc != GASTAR_OK) return -rc;
     set_grid_minw(p, mw, b->cfg.heuristic);
     p.d_weights = d;

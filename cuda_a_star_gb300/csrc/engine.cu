@@ -161,9 +161,11 @@ int launch_search(gastar_ctx* /*c: the current device's context*/, uint32_t kind
 }
 
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
-                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st) {
-    const uint32_t t = 64;
-    path_kernel<<<(n + t - 1) / t, t, 0, st>>>(d_insts, n, arena, arena_words, used);
+                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st,
+                 const unsigned long long* offs) {
+    const size_t smem = (size_t)kPathWarps * kPathWin * kPathWin * sizeof(unsigned long long);
+    path_kernel<<<(n + kPathWarps - 1) / kPathWarps, kPathWarps * 32, smem, st>>>(d_insts, n, arena, arena_words,
+                                                                                 used, offs);
     GA_CUDA(cudaGetLastError());
     return GASTAR_OK;
 }
@@ -297,6 +299,12 @@ gastar_ctx* gastar_create(int device) {
     c->coop = prop.cooperativeLaunch;
     c->smem_per_sm = prop.sharedMemPerMultiprocessor;
     c->smem_optin = prop.sharedMemPerBlockOptin;
+    {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        c->host_direct = pageable == 1 && host_tables == 1 && !std::getenv("GASTAR_NO_HOST_DIRECT");
+    }
     if (!cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreate(&c->e0), "cudaEventCreate") ||
         !cuda_ok(cudaEventCreate(&c->e1), "cudaEventCreate") ||
@@ -744,14 +752,12 @@ int gastar_solve_grid(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weig
     }
     if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
     const size_t cells = (size_t)w * h;
-    const uint32_t minw = min_passable_weight(weights, (size_t)w * h);
-    gastar_config dc;
-    gastar_config_default(&dc);
     cudaStream_t st = (cfg && cfg->stream) ? (cudaStream_t)cfg->stream : c->stream;
     if (!c->weights.ensure(cells)) return GASTAR_OUT_OF_MEMORY;
-    if (!cuda_ok(cudaMemcpyAsync(c->weights.p, weights, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
-        return GASTAR_CUDA_ERROR;
-    int rc = solve_grid_impl(c, w, h, reinterpret_cast<const uint8_t*>(c->weights.p), minw, sx, sy, tx,
+    uint32_t minw = 255;
+    int rc = upload_grid(c, reinterpret_cast<uint8_t*>(c->weights.p), weights, cells, st, &minw);
+    if (rc != GASTAR_OK) return rc;
+    rc = solve_grid_impl(c, w, h, reinterpret_cast<const uint8_t*>(c->weights.p), minw, sx, sy, tx,
                              ty, cfg, path, path_cap, out, t0);
     out->h2d_bytes += cells;
     return rc;
@@ -775,6 +781,16 @@ int gastar_solve_grid_device(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_
     int rc = device_min_weight(c, d_weights, (uint64_t)w * h, st, &minw);
     if (rc != GASTAR_OK) return rc;
     return solve_grid_impl(c, w, h, d_weights, minw, sx, sy, tx, ty, cfg, path, path_cap, out, t0);
+}
+
+int gastar_grid_min_weight(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weights, uint32_t* minw,
+                           int* host_direct) {
+    if (!c || !weights || !minw || !w || !h) return GASTAR_BAD_INPUT;
+    if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
+    const size_t cells = (size_t)w * h;
+    if (!c->weights.ensure(cells)) return GASTAR_OUT_OF_MEMORY;
+    if (host_direct) *host_direct = c->host_direct ? 1 : 0;
+    return upload_grid(c, reinterpret_cast<uint8_t*>(c->weights.p), weights, cells, c->stream, minw);
 }
 
 }  // extern "C"

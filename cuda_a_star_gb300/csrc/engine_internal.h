@@ -31,8 +31,12 @@ size_t block_smem_bytes(uint32_t kinds, uint32_t warps, uint32_t ew, bool multi,
                         uint32_t heap_snodes = kHeapSmemNodes, bool buckets = false);
 int launch_search(struct ::gastar_ctx* c, uint32_t kinds, const LaunchParams& P, uint32_t blocks,
                   uint32_t threads, size_t smem, cudaStream_t st);
+// Rebuilds the paths of finished instances into `arena` (see path_kernel):
+// with `offs` (device, n + 1 prefix offsets) each instance writes its own
+// slice in one walk.
 int launch_paths(const InstDesc* d_insts, uint32_t n, unsigned long long* arena,
-                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st);
+                 unsigned long long arena_words, unsigned long long* used, cudaStream_t st,
+                 const unsigned long long* offs = nullptr);
 // Largest count of shared-memory heap nodes per warp (>= kHeapSmemNodes) that
 // keeps `blocks_per_sm` blocks of this shape resident; *smem = the block's
 // dynamic shared memory with it.
@@ -41,6 +45,13 @@ uint32_t fit_heap_snodes(gastar_ctx* c, uint32_t kinds, uint32_t warps, uint32_t
 int occupancy_blocks(struct ::gastar_ctx* c, uint32_t kinds, uint32_t threads, size_t smem);
 int device_min_weight(struct ::gastar_ctx* c, const uint8_t* d_w, uint64_t cells, cudaStream_t st,
                       uint32_t* out);
+// Places a grid's weights from the caller's host buffer at d_dst and returns
+// its least passable weight (255: none); synchronises `st`, so the caller may
+// reuse the buffer afterwards.  Where the GPU reads pageable host memory
+// through the host's page tables, one kernel copies and reduces in a single
+// pass; elsewhere a copy, then device_min_weight.
+int upload_grid(struct ::gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint64_t cells, cudaStream_t st,
+                uint32_t* minw);
 
 struct PlainProblem {
     uint32_t kind, n;
@@ -81,6 +92,8 @@ struct gastar_ctx {
     gastar::DevBuf launch;
     void* h_launch = nullptr;      // pinned
     uint64_t* h_path = nullptr;    // pinned: the path's first words, read back with the control block
+    bool host_direct = false;      // kernels read pageable host memory through the host's
+                                   // page tables (ATS over NVLink-C2C on Grace)
     bool table_dirty = true;       // hash table needs a full clear before the next solve
     uint32_t prev_slot_words = 2;  // slot width of the solve that filled the touched list
     uint64_t launches = 0;         // kernels launched by this context

@@ -167,7 +167,7 @@ extern "C" int gastar_solve_sliding_noalloc(uint32_t n, const uint8_t* start, co
     out->d2h_bytes = sizeof(ctl);
     if (ctl.status == ST_OK && path) {
         path_kernel<<<1, 32, 0, st>>>(P.insts, 1, reinterpret_cast<unsigned long long*>(b + kPathOff),
-                                      kPathWords, used);
+                                      kPathWords, used, nullptr);  // 8-puzzle: no grid window
         if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "path_kernel");
         out->launches = 2;
         if ((e = cudaMemcpyAsync(&ctl, b + kCtlOff, sizeof(ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||

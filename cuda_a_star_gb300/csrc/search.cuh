@@ -1179,16 +1179,16 @@ __global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
     }
 }
 
-// Path rebuild (a_star.h:268-281 walked one <<<1,1>>> launch per step): one
-// thread per finished instance follows parent moves from the goal to the
-// start and writes the states goal-first.  An instance that has the arena to
-// itself (a launch of one) writes as it walks; otherwise it walks twice --
-// once to count, once to write into a slice of the shared arena reserved
-// with one atomic.  Each step is a dependent table read, so one walk instead
-// of two halves the time of long paths (a 4096^2 grid's runs to ~9k steps).
+// Path rebuild (a_star.h:268-281 walked one <<<1,1>>> launch per step): for
+// each finished puzzle one thread follows parent moves from the goal to the
+// start and writes the states goal-first (grids: walk_grid_path, a warp per
+// instance).  An instance that has the arena to itself (a launch of one)
+// writes as it walks; otherwise it walks twice -- once to count, once to
+// write into a slice of the shared arena reserved with one atomic.
 template <class D>
 __device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long long* arena,
-                          unsigned long long arena_words, unsigned long long* arena_used, bool own_arena) {
+                          unsigned long long arena_words, unsigned long long* arena_used, bool own_arena,
+                          unsigned long long base_off = 0) {
     InstCtl* ctl = d.ctl;
     const typename D::Tab tab = D::make_tab(d);
     // Every step lowers g by at least 1, so a walk longer than best + 1 states
@@ -1218,7 +1218,7 @@ __device__ void walk_path(const InstDesc& d, typename D::Ctx& ctx, unsigned long
             k = D::parent(ctx, tab, k, m);
         }
         ctl->path_len = (uint32_t)len;
-        ctl->path_off = 0;
+        ctl->path_off = base_off;
         atomicAdd(arena_used, (unsigned long long)(len * D::KW));
         return;
     }
@@ -1256,37 +1256,162 @@ template <int N> __device__ void sliding_ctx_min(typename SlidingDom<N>::Ctx& c,
     c.start = SlidingDom<N>::desc_key(d.start0, d.start1);
 }
 
-static __global__ void path_kernel(const InstDesc* insts, uint32_t n, unsigned long long* arena,
-                            unsigned long long arena_words, unsigned long long* arena_used) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// Grid path rebuild by one warp.  A dependent table load per step costs a
+// DRAM round trip (~0.6 us; a 8192^2 grid's path has ~9k steps), so the warp
+// loads the values of a kPathWin x kPathWin window of cells in one round
+// trip (lane j reads column j of every row, 32 loads in flight) into shared
+// memory, and lane 0 follows parent moves inside it.  Parents lead toward the
+// start, so the window is placed with the current cell kPathMargin cells from
+// its edge away from the start: up to ~28 steps per load.
+constexpr int kPathWin = 32, kPathMargin = 3, kPathWarps = 4;
+
+static __device__ __forceinline__ int path_win_origin(int c, int s, int n) {
+    int o = s < c ? c - (kPathWin - 1 - kPathMargin) : s > c ? c - kPathMargin : c - kPathWin / 2;
+    if (o > n - kPathWin) o = n - kPathWin;
+    return o < 0 ? 0 : o;
+}
+
+// Walks the grid path of `d` from the goal to the start (the whole warp
+// calls it).  With `out`, lane 0 writes the cells goal-first, at most `cap`
+// of them (`capped` is set when there were more).  Returns the number of
+// states, or 0 for a damaged table: a cell without a move, a move leaving the
+// grid, or more than `limit` states.
+static __device__ uint64_t walk_grid_warp(const InstDesc& d, unsigned long long* win, unsigned long long* out,
+                                   uint64_t cap, uint64_t limit, int lane, bool& capped) {
+    const int W = (int)d.W, H = (int)d.H;
+    const int sx = (int)(d.start0 % d.W), sy = (int)(d.start0 / d.W);
+    int cx = (int)(d.goal0 % d.W), cy = (int)(d.goal0 / d.W);
+    unsigned long long len = 0;
+    int state = 0;  // 0: walking, 1: at the start, 2: damaged table
+    bool cp = false;
+    while (state == 0) {
+        const int x0 = path_win_origin(cx, sx, W), y0 = path_win_origin(cy, sy, H);
+        const int x = x0 + lane;
+        unsigned long long v[kPathWin];
+#pragma unroll
+        for (int r = 0; r < kPathWin; ++r)
+            v[r] = (x < W && y0 + r < H) ? __ldcg(d.table + (size_t)(y0 + r) * W + x) : kEmpty;
+#pragma unroll
+        for (int r = 0; r < kPathWin; ++r) win[r * kPathWin + lane] = v[r];
+        __syncwarp();
+        if (lane == 0) {
+            for (;;) {  // (cx, cy) lies inside the grid and the window here
+                if (out) {
+                    if (len < cap) out[len] = (unsigned long long)cy * W + cx;
+                    else cp = true;
+                }
+                ++len;
+                if (cx == sx && cy == sy) {
+                    state = 1;
+                    break;
+                }
+                const unsigned long long t = win[(cy - y0) * kPathWin + (cx - x0)];
+                const uint32_t m = (uint32_t)t;
+                if (len > limit || t == kEmpty || m >= 8) {
+                    state = 2;
+                    break;
+                }
+                cx -= GridDom::dx((int)m);
+                cy -= GridDom::dy((int)m);
+                if (cx < 0 || cx >= W || cy < 0 || cy >= H) {
+                    state = 2;
+                    break;
+                }
+                if (cx < x0 || cx >= x0 + kPathWin || cy < y0 || cy >= y0 + kPathWin) break;
+            }
+        }
+        state = __shfl_sync(kFull, state, 0);
+        cx = __shfl_sync(kFull, cx, 0);
+        cy = __shfl_sync(kFull, cy, 0);
+        len = __shfl_sync(kFull, len, 0);
+        __syncwarp();  // the window is rewritten next
+    }
+    capped = __shfl_sync(kFull, (int)cp, 0) != 0;
+    return state == 1 ? len : 0;
+}
+
+// walk_path for grids, by a whole warp (same arena protocol and statuses).
+static __device__ void walk_grid_path(const InstDesc& d, unsigned long long* win, unsigned long long* arena,
+                               unsigned long long arena_words, unsigned long long* arena_used, bool own_arena,
+                               int lane, unsigned long long base_off) {
+    InstCtl* ctl = d.ctl;
+    const uint64_t limit = (uint64_t)ctl->best + 2;
+    bool capped = false;
+    if (own_arena) {
+        const uint64_t len = walk_grid_warp(d, win, arena, arena_words, limit, lane, capped);
+        if (lane != 0) return;
+        if (!len || capped) {  // the host retries with room for best + 1 states
+            ctl->status = ST_PATH_CAP;
+            ctl->path_len = 0;
+            return;
+        }
+        ctl->path_len = (uint32_t)len;
+        ctl->path_off = base_off;
+        atomicAdd(arena_used, (unsigned long long)len);
+        return;
+    }
+    const uint64_t len = walk_grid_warp(d, win, nullptr, 0, limit, lane, capped);
+    if (!len) {
+        if (lane == 0) {
+            ctl->status = ST_PATH_CAP;
+            ctl->path_len = 0;
+        }
+        return;
+    }
+    unsigned long long off = 0;
+    if (lane == 0) {
+        off = atomicAdd(arena_used, (unsigned long long)len);
+        ctl->path_len = (uint32_t)len;
+    }
+    off = __shfl_sync(kFull, off, 0);
+    if (off + len > arena_words) {
+        if (lane == 0) ctl->status = ST_PATH_CAP;
+        return;
+    }
+    if (lane == 0) ctl->path_off = off;
+    walk_grid_warp(d, win, arena + off, len, limit, lane, capped);
+}
+
+// One warp per finished instance: grids walk windows (walk_grid_path),
+// puzzles walk on lane 0.  Blocks of kPathWarps warps, a window of shared
+// memory per warp.  With `offs` (n + 1 prefix offsets) instance i owns arena
+// words [offs[i], offs[i+1]) and writes as it walks; otherwise a launch of
+// one owns the arena and larger launches reserve slices with an atomic.
+static __global__ void __launch_bounds__(kPathWarps * 32)
+    path_kernel(const InstDesc* insts, uint32_t n, unsigned long long* arena, unsigned long long arena_words,
+                unsigned long long* arena_used, const unsigned long long* offs) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * kPathWarps + warp;
+    if (i >= n) return;  // warp-uniform from here on: every lane reads the same instance
     const InstDesc& d = insts[i];
     if (d.ctl->life != LIFE_DONE || d.ctl->status != ST_OK) return;
+    const bool own = offs || n == 1;
+    const unsigned long long base = offs ? offs[i] : 0ull;
+    unsigned long long* a = arena + base;
+    const unsigned long long words = offs ? offs[i + 1] - base : arena_words;
+    if (d.kind == KIND_GRID) {
+        unsigned long long* win = reinterpret_cast<unsigned long long*>(g_dyn_smem) + warp * kPathWin * kPathWin;
+        walk_grid_path(d, win, a, words, arena_used, own, lane, base);
+        return;
+    }
+    if (lane != 0) return;
     switch (d.kind) {
         case KIND_SLIDING3: {
             SlidingDom<3>::Ctx c;
             sliding_ctx_min<3>(c, d);
-            walk_path<SlidingDom<3>>(d, c, arena, arena_words, arena_used, n == 1);
+            walk_path<SlidingDom<3>>(d, c, a, words, arena_used, own, base);
             break;
         }
         case KIND_SLIDING4: {
             SlidingDom<4>::Ctx c;
             sliding_ctx_min<4>(c, d);
-            walk_path<SlidingDom<4>>(d, c, arena, arena_words, arena_used, n == 1);
+            walk_path<SlidingDom<4>>(d, c, a, words, arena_used, own, base);
             break;
         }
         case KIND_SLIDING5: {
             SlidingDom<5>::Ctx c;
             sliding_ctx_min<5>(c, d);
-            walk_path<SlidingDom<5>>(d, c, arena, arena_words, arena_used, n == 1);
-            break;
-        }
-        case KIND_GRID: {
-            GridDom::Ctx c;
-            c.W = d.W;
-            c.goal = (uint32_t)d.goal0;
-            c.start = (uint32_t)d.start0;
-            walk_path<GridDom>(d, c, arena, arena_words, arena_used, n == 1);
+            walk_path<SlidingDom<5>>(d, c, a, words, arena_used, own, base);
             break;
         }
         default:

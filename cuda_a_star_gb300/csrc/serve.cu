@@ -86,6 +86,7 @@ struct Request {
     InstCtl ctl{};
     uint64_t prior_expansions = 0;
     uint32_t prior_iterations = 0;
+    uint64_t w_off = 0, w_bytes = 0;  // grid weights placed in the weights pool at submission
     std::vector<unsigned long long> path;  // goal first
 };
 
@@ -95,11 +96,15 @@ struct gastar_server {
     gastar_ctx* ctx = nullptr;
     gastar_serve_config cfg;
     DevBuf arena, descs, ctls, order, counters, path_descs, path_arena, team_ctl, team_stage;
+    // Grid weights of submitted requests, copied from the caller's buffer at
+    // submission (an eighth of the budget, outside it; a host copy when full).
+    DevBuf wpool;
+    RangeAlloc walloc;
     uint32_t heavy_teams = 0;   // team buffers allocated (the most teams a launch can hold)
     uint32_t resident = 0;      // blocks resident on the device at once
     uint64_t heavy_stage_bytes = 0;
     uint32_t heap_snodes = kHeapSmemNodes;  // shared-memory heap nodes per warp
-    RangeAlloc alloc;
+    RangeAlloc alloc;  // the arena
     uint32_t max_active = 0, threads = 0;
     size_t smem = 0;
     std::vector<InstDesc> h_desc;
@@ -117,7 +122,7 @@ struct gastar_server {
 
 namespace {
 
-PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool heavy) {
+PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool heavy, bool own_weights) {
     PartConfig pc;
     pc.warps = s->cfg.warps_per_block * (heavy ? s->cfg.heavy_team : 1);
     pc.ew = s->cfg.expansion_width;
@@ -127,7 +132,7 @@ PartConfig serve_part_config(const gastar_server* s, uint32_t retry_level, bool 
     pc.delta_grid = s->cfg.delta_grid;
     pc.sliding_states = s->cfg.sliding_states;
     pc.retry_level = retry_level;
-    pc.own_weights = true;
+    pc.own_weights = own_weights;
     pc.heap_snodes = s->heap_snodes;
     pc.buckets = s->cfg.open_list == 1;
     return pc;
@@ -140,13 +145,20 @@ void finish_request(gastar_server* s, Request& r, const InstCtl& c) {
     r.state = DONE;
     r.t_done = Clock::now();
     ++s->completed;
+    if (r.w_bytes) {  // weights placed at submission
+        s->walloc.release(r.w_off, r.w_bytes);
+        r.w_bytes = 0;
+        r.prob.d_weights = nullptr;
+    }
 }
 
-int64_t submit(gastar_server* s, Problem&& p) {
+int64_t submit(gastar_server* s, Problem&& p, Clock::time_point t0, uint64_t w_off = 0, uint64_t w_bytes = 0) {
     const int64_t id = s->next_id++;
     Request r;
     r.prob = std::move(p);
-    r.t_submit = Clock::now();
+    r.t_submit = t0;
+    r.w_off = w_off;
+    r.w_bytes = w_bytes;
     r.heavy = s->heavy_teams && r.prob.kind == KIND_GRID &&
               (uint64_t)r.prob.W * r.prob.H >= s->cfg.heavy_cells;
     if (r.prob.unreachable) {
@@ -163,23 +175,39 @@ int64_t submit(gastar_server* s, Problem&& p) {
 }
 
 // Admits waiting requests in arrival order while a slot and memory are free.
+// With admit_bypass set, a request that needs at most 1/256 of the budget
+// (puzzles, small grids) may go ahead of a larger one that waits for memory;
+// larger requests keep their arrival order among themselves, so the one at
+// the head is not passed by another large one.
 int admit(gastar_server* s, cudaStream_t st) {
-    while (!s->waiting.empty() && !s->free_slots.empty()) {
-        const int64_t id = s->waiting.front();
+    const uint64_t small = s->cfg.admit_bypass ? s->arena.n / 256 : 0;
+    bool blocked = false;  // a request larger than `small` waits for memory
+    for (auto it = s->waiting.begin(); it != s->waiting.end() && !s->free_slots.empty();) {
+        const int64_t id = *it;
         Request& r = s->reqs[id];
-        const PartConfig pc = serve_part_config(s, r.retry_level, r.heavy);
+        const bool own = r.prob.kind == KIND_GRID && !r.prob.d_weights;
+        const PartConfig pc = serve_part_config(s, r.retry_level, r.heavy, own);
         const PartPlan plan = plan_partition(r.prob, pc);
         if (plan.bytes > s->arena.n) {  // can never fit the budget
-            s->waiting.pop_front();
+            it = s->waiting.erase(it);
             InstCtl c{};
             c.status = GASTAR_OUT_OF_MEMORY;
             c.life = LIFE_DONE;
             finish_request(s, r, c);
             continue;
         }
+        if (blocked && plan.bytes > small) {
+            ++it;
+            continue;
+        }
         uint64_t off;
-        if (!s->alloc.alloc(plan.bytes, off)) break;  // wait for memory to free up
-        s->waiting.pop_front();
+        if (!s->alloc.alloc(plan.bytes, off)) {  // wait for memory to free up
+            if (!small) break;
+            blocked = true;
+            ++it;
+            continue;
+        }
+        it = s->waiting.erase(it);
         const int slot = s->free_slots.back();
         s->free_slots.pop_back();
         r.slot = slot;
@@ -189,8 +217,8 @@ int admit(gastar_server* s, cudaStream_t st) {
         s->slot_req[slot] = id;
         char* base = reinterpret_cast<char*>(s->arena.p) + off;
         InstCtl* ctl = reinterpret_cast<InstCtl*>(s->ctls.p) + slot;
-        fill_desc(s->h_desc[slot], r.prob, pc, plan, base, nullptr, ctl);
-        if (r.prob.kind == KIND_GRID &&
+        fill_desc(s->h_desc[slot], r.prob, pc, plan, base, r.prob.d_weights, ctl);
+        if (own &&
             !cuda_ok(cudaMemcpyAsync(base + plan.weights_off, r.prob.weights.data(), r.prob.weights.size(),
                                      cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
             return GASTAR_CUDA_ERROR;
@@ -261,7 +289,9 @@ extern "C" {
 void gastar_serve_config_default(gastar_serve_config* c) {
     std::memset(c, 0, sizeof(*c));
     c->budget_bytes = 120ull << 30;
-    c->slice_iters = 64;
+    // 128 iterations per slice: burst capacity 205 req/s against 196 with 64
+    // and 204 with 256 (fewer steps, each with its own host round trip).
+    c->slice_iters = 128;
     c->warps_per_block = 8;
     c->expansion_width = 32;
     c->load_factor = 0.75f;
@@ -276,6 +306,8 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     // the served mix, 15-puzzle p99 34 ms and overall p99 0.74 s, against
     // 0.5 s and 1.15 s past 2^21; burst capacity unchanged (156-164 req/s).
     c->promote_log2 = 18;
+    c->admit_bypass = 1;
+    c->weights_pool = 1;
 }
 
 gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
@@ -291,7 +323,7 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
     if (!cf.expansion_width) cf.expansion_width = 32;
     cf.expansion_width = std::min(32u, cf.expansion_width);
     if (cf.load_factor <= 0.f) cf.load_factor = 0.75f;
-    if (!cf.slice_iters) cf.slice_iters = 64;
+    if (!cf.slice_iters) cf.slice_iters = 128;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     uint64_t budget = cf.budget_bytes ? cf.budget_bytes : (120ull << 30);
@@ -335,6 +367,17 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
         return nullptr;
     }
     s->alloc.reset(s->arena.n);
+    {
+        size_t f2 = 0, t2 = 0;
+        cudaMemGetInfo(&f2, &t2);
+        const uint64_t want = std::min<uint64_t>(budget / 8, f2 > (4ull << 30) ? f2 - (4ull << 30) : 0);
+        if (cf.weights_pool && want >= (16ull << 20) && s->wpool.ensure(want)) {
+            s->walloc.reset(s->wpool.n);
+        } else {  // no pool: grids keep host copies
+            cudaGetLastError();
+            s->wpool.release();
+        }
+    }
     s->h_desc.assign(m, InstDesc());
     s->slot_req.assign(m, -1);
     for (int i = (int)m - 1; i >= 0; --i) s->free_slots.push_back(i);
@@ -356,6 +399,7 @@ void gastar_serve_destroy(gastar_server* s) {
     s->path_arena.release();
     s->team_ctl.release();
     s->team_stage.release();
+    s->wpool.release();
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
     if (s->e0) cudaEventDestroy(s->e0);
     if (s->e1) cudaEventDestroy(s->e1);
@@ -365,22 +409,46 @@ void gastar_serve_destroy(gastar_server* s) {
 int64_t gastar_serve_submit_sliding(gastar_server* s, uint32_t n, const uint8_t* start, const uint8_t* goal) {
     if (!s) return -GASTAR_BAD_INPUT;
     Problem p;
+    const Clock::time_point t0 = Clock::now();
     if (!make_sliding_problem(n, start, goal, s->cfg.heuristic, s->cfg.moves, p)) {
         set_error("sliding: boards must be permutations of 0..n*n-1 with n in 3..5");
         return -GASTAR_BAD_INPUT;
     }
-    return submit(s, std::move(p));
+    return submit(s, std::move(p), t0);
 }
 
 int64_t gastar_serve_submit_grid(gastar_server* s, uint32_t w, uint32_t h, const uint8_t* weights,
                                  uint32_t sx, uint32_t sy, uint32_t tx, uint32_t ty) {
     if (!s) return -GASTAR_BAD_INPUT;
+    const Clock::time_point t0 = Clock::now();
     Problem p;
-    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, s->cfg.heuristic, p)) {
+    if (!make_grid_problem(w, h, weights, sx, sy, tx, ty, s->cfg.heuristic, p, false)) {
         set_error("grid: bad dimensions or endpoints");
         return -GASTAR_BAD_INPUT;
     }
-    return submit(s, std::move(p));
+    // The weights go from the caller's buffer to the weights pool and their
+    // least passable weight is reduced there (a host copy's first-touch page
+    // faults cost more than the transfer); a full pool keeps a host copy,
+    // copied at admission.
+    const uint64_t cells = (uint64_t)w * h, wb = (cells + 255) & ~255ull;
+    uint64_t off = 0;
+    if (s->wpool.n && s->walloc.alloc(wb, off)) {
+        if (cudaSetDevice(s->ctx->device) != cudaSuccess) return -GASTAR_CUDA_ERROR;
+        cudaStream_t st = s->ctx->stream;
+        uint8_t* d = reinterpret_cast<uint8_t*>(s->wpool.p) + off;
+        uint32_t mw = 255;
+        const int rc = upload_grid(s->ctx, d, weights, cells, st, &mw);
+        if (rc != GASTAR_OK) {
+            s->walloc.release(off, wb);
+            return -rc;
+        }
+        set_grid_minw(p, mw, s->cfg.heuristic);
+        p.d_weights = d;
+        return submit(s, std::move(p), t0, off, wb);
+    }
+    p.weights.assign(weights, weights + cells);
+    set_grid_minw(p, min_passable_weight(weights, cells), s->cfg.heuristic);
+    return submit(s, std::move(p), t0);
 }
 
 int gastar_serve_step(gastar_server* s) {
@@ -489,22 +557,32 @@ int gastar_serve_step(gastar_server* s) {
     }
     for (auto it = requeue.rbegin(); it != requeue.rend(); ++it) s->waiting.push_front(*it);
     if (!solved.empty()) {
-        std::vector<InstDesc> pd;
+        // Descriptors, then each path's slice of the arena (best + 1 states
+        // at most, every step lowering g by at least 1), in one upload: the
+        // paths are written in a single walk each.
+        const uint32_t m = (uint32_t)solved.size();
+        const size_t desc_bytes = (sizeof(InstDesc) * m + 7) & ~size_t(7);
+        std::vector<unsigned char> up(desc_bytes + 8 * (size_t)(m + 1));
+        unsigned long long* offs = reinterpret_cast<unsigned long long*>(up.data() + desc_bytes);
         uint64_t words = 0;
-        for (uint32_t slot : solved) {
-            pd.push_back(s->h_desc[slot]);
+        for (uint32_t k = 0; k < m; ++k) {
+            const uint32_t slot = solved[k];
+            std::memcpy(up.data() + sizeof(InstDesc) * k, &s->h_desc[slot], sizeof(InstDesc));
+            offs[k] = words;
             words += ((uint64_t)s->h_ctl[slot].best + 2) * key_words(s->h_desc[slot].kind);
         }
-        const uint32_t m = (uint32_t)pd.size();
-        if (!s->path_descs.ensure(sizeof(InstDesc) * m) || !s->path_arena.ensure(words * 8 + 16))
+        offs[m] = words;
+        if (!s->path_descs.ensure(up.size()) || !s->path_arena.ensure(words * 8 + 16))
             return GASTAR_OUT_OF_MEMORY;
         unsigned long long* used = reinterpret_cast<unsigned long long*>(s->counters.p) + 2;
-        if (!cuda_ok(cudaMemcpyAsync(s->path_descs.p, pd.data(), sizeof(InstDesc) * m,
-                                     cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
+        if (!cuda_ok(cudaMemcpyAsync(s->path_descs.p, up.data(), up.size(), cudaMemcpyHostToDevice, st),
+                     "cudaMemcpyAsync") ||
             !cuda_ok(cudaMemsetAsync(used, 0, 8, st), "cudaMemsetAsync"))
             return GASTAR_CUDA_ERROR;
         rc = launch_paths(reinterpret_cast<const InstDesc*>(s->path_descs.p), m,
-                          reinterpret_cast<unsigned long long*>(s->path_arena.p), words, used, st);
+                          reinterpret_cast<unsigned long long*>(s->path_arena.p), words, used, st,
+                          reinterpret_cast<const unsigned long long*>(
+                              reinterpret_cast<const char*>(s->path_descs.p) + desc_bytes));
         if (rc != GASTAR_OK) return rc;
         std::vector<unsigned long long> arena(words);
         if (!cuda_ok(cudaMemcpyAsync(s->h_ctl, s->ctls.p, sizeof(InstCtl) * s->max_active,

@@ -134,6 +134,16 @@ int gastar_solve_grid_device(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint
                              const gastar_config *cfg, uint32_t *path, uint32_t path_cap,
                              gastar_result *out);
 
+/* The least passable (non-zero) weight of a grid, 255 if none: the factor of
+ * the admissible grid heuristic.  The weights reach the device as in
+ * gastar_solve_grid: read in place by a kernel where the GPU reads pageable
+ * host memory through the host's page tables (*host_direct = 1; Grace
+ * systems; the environment variable GASTAR_NO_HOST_DIRECT at gastar_create
+ * turns it off), else copied.  host_direct may be NULL.  No counterpart in
+ * the reference (its grid heuristic takes no weight factor). */
+int gastar_grid_min_weight(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint8_t *weights,
+                           uint32_t *minw, int *host_direct);
+
 /* 8-puzzle solve that allocates nothing, for callers that cannot call
  * cudaMalloc (their device memory is reserved by another pool, or they must
  * avoid the device-wide synchronisation of cudaMalloc/cudaFree).  No
@@ -232,7 +242,7 @@ typedef struct gastar_server gastar_server;
 typedef struct gastar_serve_config {
     uint64_t budget_bytes;     /* device bytes for request partitions (default 120 GiB) */
     uint32_t max_active;       /* requests on the device at once (0 = resident blocks) */
-    uint32_t slice_iters;      /* iterations per request per step */
+    uint32_t slice_iters;      /* iterations per request per step (default 128) */
     uint32_t warps_per_block;  /* warp-heaps per request */
     uint32_t expansion_width;  /* pops per warp-heap per iteration */
     float load_factor;
@@ -251,6 +261,13 @@ typedef struct gastar_serve_config {
                                   expansions leaves its slot and is finished by the plain
                                   engine on the whole GPU between two steps (0 = never;
                                   default 18) */
+    uint32_t admit_bypass;     /* 1 (default) = a request needing at most 1/256 of the
+                                  budget may be admitted ahead of a larger one waiting
+                                  for memory; 0 = strict arrival order */
+    uint32_t weights_pool;     /* 1 (default) = grid weights go from the caller's buffer
+                                  to a device pool (an eighth of the budget, beside it)
+                                  at submission; 0, or a full pool = a host copy, sent
+                                  at admission */
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);

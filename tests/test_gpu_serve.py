@@ -126,3 +126,51 @@ def test_hard_puzzles_promoted_to_the_plain_engine(engine, oracle, gastar):
         _check(oracle, r, out[i])
     # at least the 15-puzzles passed 2^12 expansions (and were promoted)
     assert sum(out[i].expansions > (1 << 12) for i in ids[:6]) >= 3
+
+
+def test_grid_weights_in_the_pool_and_host_copies(engine, oracle, gastar):
+    """Grid weights go from the caller's buffer to the device pool at
+    submission (an eighth of the budget: 32 MiB here); once 32 grids of 1 MB
+    fill it, later ones keep a host copy sent at admission.  Both kinds match
+    the oracle, and a server without a pool returns the same costs."""
+    reqs = []
+    for i in range(40):
+        w, h = 1000 + (i % 3), 1000 + (i % 5)
+        reqs.append(("g", gastar.gen_grid(w, h, 7000 + i, 0.2), (0, 0), (w - 1, h - 1)))
+    res = {}
+    for pool in (1, 0):
+        srv = engine.server(budget_bytes=256 << 20, slice_iters=32, weights_pool=pool)
+        ids = [_submit(srv, r) for r in reqs]
+        out = srv.drain(ids)
+        srv.close()
+        res[pool] = [out[i] for i in ids]
+        for k, r in enumerate(reqs):
+            # every grid's weights arrays may be reused by the caller now
+            assert res[pool][k].status_name == "OK"
+    _, ref = oracle.grid_batch([r[1:] for r in reqs])
+    for k, (r, o) in enumerate(zip(reqs, ref)):
+        assert res[1][k].cost == res[0][k].cost == o.cost
+        assert oracle.grid_validate(r[1], r[2], r[3], res[1][k].path) == (True, o.cost)
+
+
+def test_small_requests_pass_a_large_one_waiting_for_memory(engine, oracle, gastar):
+    """20 grids of 3000^2 need more than the 4 GiB budget, so some wait for
+    memory; 64^2 grids submitted after them (partitions under 1/256 of the
+    budget) are admitted at once with admit_bypass, and wait behind the
+    large ones in strict arrival order.  Results are the same either way."""
+    big = [("g", gastar.gen_grid(3000, 3000, 7100 + i, 0.2), (0, 0), (2999, 2999)) for i in range(20)]
+    small = [("g", gastar.gen_grid(64, 64, 7200 + i, 0.2), (0, 0), (63, 63)) for i in range(8)]
+    waiting, res = {}, {}
+    for bypass in (1, 0):
+        srv = engine.server(budget_bytes=4 << 30, admit_bypass=bypass)
+        ids = [_submit(srv, r) for r in big + small]
+        srv.step()
+        waiting[bypass] = srv.stats()["waiting"]
+        out = srv.drain(ids)
+        srv.close()
+        res[bypass] = [out[i] for i in ids]
+    assert waiting[1] >= 1  # a large grid waits for memory
+    assert waiting[0] == waiting[1] + len(small)
+    assert [(r.status, r.cost) for r in res[1]] == [(r.status, r.cost) for r in res[0]]
+    for k, r in enumerate(small):
+        _check(oracle, r, res[1][len(big) + k])
