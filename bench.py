@@ -568,14 +568,18 @@ def run_served(g, eng, check: bool = True) -> dict:
         return srv.submit_sliding(r[1], r[2]) if r[0] == "s" else srv.submit_grid(r[1], r[2], r[3])
 
     def run(arrivals, paths=False):
+        k0 = srv.stats()["kernel_ms"]
         t0 = time.perf_counter()
         ids, res, nxt = {}, {}, 0
         order = np.argsort(arrivals, kind="stable")
         pending = set()
+        t_submit = 0.0
         while len(res) < len(reqs):
             now = time.perf_counter() - t0
             while nxt < len(order) and arrivals[order[nxt]] <= now:
+                ts = time.perf_counter()
                 i = submit(reqs[order[nxt]])
+                t_submit += time.perf_counter() - ts
                 ids[i] = int(order[nxt])
                 pending.add(i)
                 nxt += 1
@@ -590,10 +594,12 @@ def run_served(g, eng, check: bool = True) -> dict:
                     res[ids[i]] = r
                     pending.discard(i)
         wall = time.perf_counter() - t0
+        kernel_s = (srv.stats()["kernel_ms"] - k0) / 1000.0
         for i in ids:
             srv.release(i)
         lat = [res[k].total_ms for k in range(len(reqs))]
         out = {"solves_per_s": len(reqs) / wall, "wall_s": wall,
+               "submit_s": t_submit, "search_kernel_s": kernel_s,
                "node_expansions_per_s": sum(r.expansions for r in res.values()) / wall,
                "latency_ms": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99)},
                "latency_ms_by_class": {
