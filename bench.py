@@ -849,7 +849,8 @@ def run_ours(args) -> dict:
 def run_profile_case(kind: str) -> None:
     """Small copies of the workloads for ncu captures (a few GB on the device).
     plain: 4 of the 64 P15 instances, 2^24-slot table, one launch each.
-    batched: 32 P15 (walk 20-80) + 32 grids (side 256-512), a run and a re-run."""
+    batched: 32 P15 (walk 20-80) + 32 grids (side 256-512), a run and a re-run.
+    grid: the 4096^2 grid solved twice (upload kernel, search, path rebuild)."""
     import cuda_a_star_gb300 as g
     from cuda_a_star_gb300 import build as engine_build
     engine_build.build()
@@ -866,6 +867,15 @@ def run_profile_case(kind: str) -> None:
                                   "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
                                   "iterations": r.iterations, "kernel_ms": r.kernel_ms,
                                   "algorithmic_bytes": alg(r)}))
+            return
+        if kind == "grid":
+            wts = g.gen_grid(4096, 4096, 0x4096, 0.2)
+            for _ in range(2):
+                r = eng.solve_grid(wts, (0, 0), (4095, 4095), num_queues=16384, delta=GRID_DELTA_PLAIN,
+                                   path=True)
+                print(json.dumps({"status": r.status_name, "cost": r.cost, "path_len": len(r.path),
+                                  "kernel_ms": r.kernel_ms, "total_ms": r.total_ms,
+                                  "weights_read_in_place": eng.grid_min_weight(wts[:16, :16])[1]}))
             return
         p15, grids = _mixed_instances(g)
         b = eng.batch(warps_per_block=16, expansion_width=32, load_factor=0.5, delta_grid=18)
@@ -900,7 +910,7 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the reference's own CUDA GA* beside the engine on small grids")
     ap.add_argument("--reference-gpu-case", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--profile-case", nargs="?", const="plain", choices=["plain", "batched"],
+    ap.add_argument("--profile-case", nargs="?", const="plain", choices=["plain", "batched", "grid"],
                     help="small single pass for ncu captures (no bench JSON line)")
     ap.add_argument("--random-sweep", action="store_true",
                     help="print the random-access rate over buffer size, depth in flight and "
