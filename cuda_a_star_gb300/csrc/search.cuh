@@ -1264,6 +1264,9 @@ template <int N> __device__ void sliding_ctx_min(typename SlidingDom<N>::Ctx& c,
 // start, so the window is placed with the current cell kPathMargin cells from
 // its edge away from the start: up to ~28 steps per load.
 constexpr int kPathWin = 32, kPathMargin = 3, kPathWarps = 4;
+// GridDom::dx(m) + 1 and GridDom::dy(m) + 1 in bits 2m..2m+1.
+constexpr uint32_t kGridDxPack = 2u | 0u << 2 | 1u << 4 | 1u << 6 | 2u << 8 | 2u << 10 | 0u << 12 | 0u << 14;
+constexpr uint32_t kGridDyPack = 1u | 1u << 2 | 2u << 4 | 0u << 6 | 2u << 8 | 0u << 10 | 2u << 12 | 0u << 14;
 
 static __device__ __forceinline__ int path_win_origin(int c, int s, int n) {
     int o = s < c ? c - (kPathWin - 1 - kPathMargin) : s > c ? c - kPathMargin : c - kPathWin / 2;
@@ -1295,30 +1298,39 @@ static __device__ uint64_t walk_grid_warp(const InstDesc& d, unsigned long long*
         for (int r = 0; r < kPathWin; ++r) win[r * kPathWin + lane] = v[r];
         __syncwarp();
         if (lane == 0) {
-            for (;;) {  // (cx, cy) lies inside the grid and the window here
+            // Window-local coordinates; a step is one shared-memory load and
+            // a few integer operations (dx, dy from 2-bit fields).  Inside
+            // the window a cell outside the grid holds kEmpty (loaded so), so
+            // the grid bounds are checked only when the walk leaves it.
+            int lx = cx - x0, ly = cy - y0;
+            const int slx = sx - x0, sly = sy - y0;
+            unsigned long long cell = (unsigned long long)cy * W + cx;
+            for (;;) {
                 if (out) {
-                    if (len < cap) out[len] = (unsigned long long)cy * W + cx;
+                    if (len < cap) out[len] = cell;
                     else cp = true;
                 }
                 ++len;
-                if (cx == sx && cy == sy) {
+                if (lx == slx && ly == sly) {
                     state = 1;
                     break;
                 }
-                const unsigned long long t = win[(cy - y0) * kPathWin + (cx - x0)];
+                const unsigned long long t = win[ly * kPathWin + lx];
                 const uint32_t m = (uint32_t)t;
                 if (len > limit || t == kEmpty || m >= 8) {
                     state = 2;
                     break;
                 }
-                cx -= GridDom::dx((int)m);
-                cy -= GridDom::dy((int)m);
-                if (cx < 0 || cx >= W || cy < 0 || cy >= H) {
-                    state = 2;
-                    break;
-                }
-                if (cx < x0 || cx >= x0 + kPathWin || cy < y0 || cy >= y0 + kPathWin) break;
+                const int dx = (int)((kGridDxPack >> (2 * m)) & 3u) - 1;
+                const int dy = (int)((kGridDyPack >> (2 * m)) & 3u) - 1;
+                lx -= dx;
+                ly -= dy;
+                cell -= (long long)dx + (long long)dy * W;
+                if ((unsigned)lx >= (unsigned)kPathWin || (unsigned)ly >= (unsigned)kPathWin) break;
             }
+            cx = x0 + lx;
+            cy = y0 + ly;
+            if (state == 0 && (cx < 0 || cx >= W || cy < 0 || cy >= H)) state = 2;
         }
         state = __shfl_sync(kFull, state, 0);
         cx = __shfl_sync(kFull, cx, 0);

@@ -18,13 +18,21 @@ DX = [1, -1, 0, 0, 1, 1, -1, -1]  # GridDom::dx
 DY = [0, 0, 1, -1, 1, -1, 1, -1]  # GridDom::dy
 
 
+SRC = open(os.path.join(ROOT, "cuda_a_star_gb300", "csrc", "search.cuh")).read()
+
+
 def _constants():
-    src = open(os.path.join(ROOT, "cuda_a_star_gb300", "csrc", "search.cuh")).read()
-    m = re.search(r"constexpr int kPathWin = (\d+), kPathMargin = (\d+)", src)
+    m = re.search(r"constexpr int kPathWin = (\d+), kPathMargin = (\d+)", SRC)
     return int(m.group(1)), int(m.group(2))
 
 
+def _pack(name):
+    expr = re.search(r"constexpr uint32_t %s = ([^;]+);" % name, SRC).group(1)
+    return eval(re.sub(r"(\d+)u", r"\1", expr))
+
+
 WIN, MARGIN = _constants()
+DXP, DYP = _pack("kGridDxPack"), _pack("kGridDyPack")
 
 
 def origin(c, s, n):
@@ -55,7 +63,7 @@ def walk(table, W, H, start, goal, limit, cap=None):
             m = t & 0xffffffff
             if n > limit or t == EMPTY or m >= 8:
                 return 0, out, loads
-            cx, cy = cx - DX[m], cy - DY[m]
+            cx, cy = cx - (((DXP >> (2 * m)) & 3) - 1), cy - (((DYP >> (2 * m)) & 3) - 1)
             if not (0 <= cx < W and 0 <= cy < H):
                 return 0, out, loads
             if not (x0 <= cx < x0 + WIN and y0 <= cy < y0 + WIN):
@@ -121,3 +129,17 @@ def test_damaged_tables_give_zero():
     table[3 * W + 3] = 4  # (3,3) <- (2,2) <- (3,3): a cycle, stopped by the limit
     table[2 * W + 2] = 7
     assert walk(table, W, H, 0, 3 * W + 3, limit=50)[0] == 0
+
+
+def test_packed_moves_match_the_grid_domain():
+    """kGridDxPack / kGridDyPack hold GridDom::dx / dy as search.cuh defines them."""
+    def sets(fn):
+        body = re.search(r"int %s\(int m\) \{ return ([^;]+);" % fn, SRC).group(1)
+        plus, minus = re.findall(r"\(([^?]+)\) \?", body)
+        return ({int(v) for v in re.findall(r"m == (\d)", plus)},
+                {int(v) for v in re.findall(r"m == (\d)", minus)})
+    for fn, pack, ref in (("dx", DXP, DX), ("dy", DYP, DY)):
+        plus, minus = sets(fn)
+        for m in range(8):
+            want = 1 if m in plus else -1 if m in minus else 0
+            assert ((pack >> (2 * m)) & 3) - 1 == want == ref[m], (fn, m)
