@@ -875,7 +875,7 @@ def run_profile_case(kind: str) -> None:
                                    path=True)
                 print(json.dumps({"status": r.status_name, "cost": r.cost, "path_len": len(r.path),
                                   "kernel_ms": r.kernel_ms, "total_ms": r.total_ms,
-                                  "weights_read_in_place": eng.grid_min_weight(wts[:16, :16])[1]}))
+                                  "upload_path": eng.grid_min_weight(wts[:16, :16])[1]}))
             return
         p15, grids = _mixed_instances(g)
         b = eng.batch(warps_per_block=16, expansion_width=32, load_factor=0.5, delta_grid=18)

@@ -162,15 +162,17 @@ class Engine:
         _check(rc, "gastar_solve_grid_device")
         return SolveResult.from_c(res, None)
 
-    def grid_min_weight(self, weights) -> tuple[int, bool]:
+    UPLOAD_PATHS = ("copy", "inplace", "staged")
+
+    def grid_min_weight(self, weights) -> tuple[int, str]:
         """Least passable weight of a grid as the engine computes it (255: none),
-        and whether the weights were read in place by the GPU."""
+        and the upload path that brought the weights to the device."""
         w8 = np.ascontiguousarray(weights, dtype=np.uint8)
         h, w = w8.shape
-        mw, direct = C.c_uint32(), C.c_int()
-        _check(lib().gastar_grid_min_weight(self._h, w, h, _u8p(w8), C.byref(mw), C.byref(direct)),
+        mw, up = C.c_uint32(), C.c_int()
+        _check(lib().gastar_grid_min_weight(self._h, w, h, _u8p(w8), C.byref(mw), C.byref(up)),
                "gastar_grid_min_weight")
-        return mw.value, bool(direct.value)
+        return mw.value, self.UPLOAD_PATHS[up.value]
 
     def random_access_peak(self, kind: str = "gather", buffer_bytes: int = 8 << 30) -> dict:
         """Measured random 32-byte-sector rate (GB/s): "gather" loads or "cas"

@@ -91,7 +91,11 @@ __global__ void copy_min_kernel(const uint8_t* __restrict__ src, uint8_t* __rest
 
 int upload_grid(gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint64_t cells, cudaStream_t st,
                 uint32_t* minw) {
-    if (!c->host_direct) {
+    if (c->upload_mode == 2) {
+        const int rc = upload_grid_staged(c, d_dst, h_src, cells, st, minw);
+        if (rc != GASTAR_OUT_OF_MEMORY) return rc;  // no pinned ring: copy
+    }
+    if (c->upload_mode != 1) {
         if (!cuda_ok(cudaMemcpyAsync(d_dst, h_src, cells, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
             return GASTAR_CUDA_ERROR;
         return device_min_weight(c, d_dst, cells, st, minw);

@@ -303,7 +303,11 @@ gastar_ctx* gastar_create(int device) {
         int pageable = 0, host_tables = 0;
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
         cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
-        c->host_direct = pageable == 1 && host_tables == 1 && !std::getenv("GASTAR_NO_HOST_DIRECT");
+        c->can_read_host = pageable == 1 && host_tables == 1;
+        // Grid uploads: staged by default; GASTAR_UPLOAD=inplace (where the
+        // GPU reads pageable host memory) or copy choose the others.
+        const char* u = std::getenv("GASTAR_UPLOAD");
+        c->upload_mode = u && !std::strcmp(u, "copy") ? 0 : u && !std::strcmp(u, "inplace") && c->can_read_host ? 1 : 2;
     }
     if (!cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreate(&c->e0), "cudaEventCreate") ||
@@ -332,6 +336,7 @@ void gastar_destroy(gastar_ctx* c) {
     c->path.release();
     c->misc.release();
     c->weights.release();
+    destroy_stager(c->stager);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_launch) cudaFreeHost(c->h_launch);
     if (c->h_path) cudaFreeHost(c->h_path);
@@ -784,12 +789,12 @@ int gastar_solve_grid_device(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_
 }
 
 int gastar_grid_min_weight(gastar_ctx* c, uint32_t w, uint32_t h, const uint8_t* weights, uint32_t* minw,
-                           int* host_direct) {
+                           int* upload_path) {
     if (!c || !weights || !minw || !w || !h) return GASTAR_BAD_INPUT;
     if (cudaSetDevice(c->device) != cudaSuccess) return GASTAR_CUDA_ERROR;
     const size_t cells = (size_t)w * h;
     if (!c->weights.ensure(cells)) return GASTAR_OUT_OF_MEMORY;
-    if (host_direct) *host_direct = c->host_direct ? 1 : 0;
+    if (upload_path) *upload_path = c->upload_mode;
     return upload_grid(c, reinterpret_cast<uint8_t*>(c->weights.p), weights, cells, c->stream, minw);
 }
 

@@ -47,11 +47,18 @@ int device_min_weight(struct ::gastar_ctx* c, const uint8_t* d_w, uint64_t cells
                       uint32_t* out);
 // Places a grid's weights from the caller's host buffer at d_dst and returns
 // its least passable weight (255: none); synchronises `st`, so the caller may
-// reuse the buffer afterwards.  Where the GPU reads pageable host memory
-// through the host's page tables, one kernel copies and reduces in a single
-// pass; elsewhere a copy, then device_min_weight.
+// reuse the buffer afterwards.  By the context's upload_mode: staged (host
+// threads and a pinned ring), read in place by one kernel that also reduces
+// (where the GPU reads pageable host memory through the host's page tables),
+// or a copy, then device_min_weight.
 int upload_grid(struct ::gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint64_t cells, cudaStream_t st,
                 uint32_t* minw);
+// The staged way (upload.cpp): host threads fill pinned chunks and reduce the
+// least weight while the previous chunks are sent.
+struct HostStager;
+int upload_grid_staged(struct ::gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint64_t cells,
+                       cudaStream_t st, uint32_t* minw);
+void destroy_stager(HostStager* s);
 
 struct PlainProblem {
     uint32_t kind, n;
@@ -92,8 +99,10 @@ struct gastar_ctx {
     gastar::DevBuf launch;
     void* h_launch = nullptr;      // pinned
     uint64_t* h_path = nullptr;    // pinned: the path's first words, read back with the control block
-    bool host_direct = false;      // kernels read pageable host memory through the host's
+    bool can_read_host = false;    // kernels read pageable host memory through the host's
                                    // page tables (ATS over NVLink-C2C on Grace)
+    int upload_mode = 2;           // grid uploads: 0 copy, 1 read in place, 2 staged
+    gastar::HostStager* stager = nullptr;  // staged uploads (pinned ring, host threads)
     bool table_dirty = true;       // hash table needs a full clear before the next solve
     uint32_t prev_slot_words = 2;  // slot width of the solve that filled the touched list
     uint64_t launches = 0;         // kernels launched by this context

@@ -136,13 +136,16 @@ int gastar_solve_grid_device(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint
 
 /* The least passable (non-zero) weight of a grid, 255 if none: the factor of
  * the admissible grid heuristic.  The weights reach the device as in
- * gastar_solve_grid: read in place by a kernel where the GPU reads pageable
- * host memory through the host's page tables (*host_direct = 1; Grace
- * systems; the environment variable GASTAR_NO_HOST_DIRECT at gastar_create
- * turns it off), else copied.  host_direct may be NULL.  No counterpart in
- * the reference (its grid heuristic takes no weight factor). */
+ * gastar_solve_grid, gastar_batch_add_grid and gastar_serve_submit_grid, by
+ * the context's upload path (*upload_path; may be NULL): 2 = staged (default:
+ * host threads copy into pinned chunks and reduce while earlier chunks are
+ * sent), 1 = read in place by one kernel (GPUs that read pageable host
+ * memory through the host's page tables, e.g. Grace systems), 0 = copied,
+ * then reduced on the device.  The environment variable GASTAR_UPLOAD
+ * (staged | inplace | copy) at gastar_create chooses.  No counterpart in the
+ * reference (its grid heuristic takes no weight factor). */
 int gastar_grid_min_weight(gastar_ctx *ctx, uint32_t w, uint32_t h, const uint8_t *weights,
-                           uint32_t *minw, int *host_direct);
+                           uint32_t *minw, int *upload_path);
 
 /* 8-puzzle solve that allocates nothing, for callers that cannot call
  * cudaMalloc (their device memory is reserved by another pool, or they must
