@@ -5,9 +5,10 @@
 //    chunks and reduce its least passable weight while they copy; each filled
 //    chunk goes to the device by DMA while the next one is copied.  The
 //    threads walk the caller's pages with the CPU's own page tables, so the
-//    rate holds on pages the GPU has never seen (measured ~25 GB/s in a
-//    Python model of it on GB300 hosts, where the driver's pageable copy ran
-//    at 3-15 GB/s and in-place reads at 7-37 GB/s on fresh pages);
+//    rate holds on pages the GPU has never seen (measured 57-59 GB/s on 3 GB
+//    of freshly generated grids on a GB300 host, where in-place reads ran at
+//    4-5 GB/s and the driver's pageable copy at 3-4 GB/s; on other hosts
+//    those two ranged 7-37 and 3-15 GB/s);
 //  * in place: one kernel reads the buffer through the host's page tables
 //    (Grace: NVLink-C2C) and reduces in the same pass (copy_min_kernel);
 //  * copy: cudaMemcpyAsync from the pageable buffer, then min_weight_kernel.
