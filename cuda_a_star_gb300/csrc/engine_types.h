@@ -214,6 +214,7 @@ struct LaunchParams {
     TeamCtl* heavy_ctl;
     void* heavy_stage;
     uint64_t heavy_stage_bytes;
+    const uint32_t* slices;   // per instance slot: iterations per slice (nullptr = slice_iters)
 };
 
 }  // namespace gastar

@@ -334,7 +334,7 @@ struct CtaShared {
     uint32_t agg_err_prev;           // heap full in the previous push
     uint32_t dec_status, dec_best, dec_fmin, push_count;  // thread 0 -> block
     InstDesc desc;
-    uint32_t inst, ok, pad0, pad1;
+    uint32_t inst, ok, slice, pad1;  // slice: iterations before suspending (0 = to the end)
     union {
         SlidingDom<3>::Ctx s3;
         SlidingDom<4>::Ctx s4;
@@ -1031,7 +1031,7 @@ __device__ __noinline__ void run_instance(const LaunchParams& P, const InstDesc&
         }
         ++it;
         have_prev = true;
-        if (P.slice_iters && it >= P.slice_iters) break;  // suspend
+        if (sm.slice && it >= sm.slice) break;  // suspend
     }
 
     if (lane == 0) atomicMax(&ctl->max_nodes, hp.max_n);
@@ -1134,7 +1134,10 @@ template <uint32_t KINDS, int MAXT = 256>
 __global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
     __shared__ CtaShared sm;
     if (P.team_ctas > 1) {
-        if (threadIdx.x == 0) sm.desc = P.insts[0];
+        if (threadIdx.x == 0) {
+            sm.desc = P.insts[0];
+            sm.slice = P.slice_iters;
+        }
         __syncthreads();
         dispatch<KINDS>(P, sm, TeamRef{P.team_ctas, blockIdx.x, P.team, P.stage});
         return;
@@ -1161,7 +1164,11 @@ __global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
             if (!team_sync_grid(tc, P.heavy_team, P.barrier_timeout_ns, sm)) break;
             const uint32_t i = ld_vol(&tc->inst);
             if (i >= P.n_heavy) break;
-            if (threadIdx.x == 0) sm.desc = P.insts[P.heavy_order[i]];
+            if (threadIdx.x == 0) {
+                const uint32_t slot = P.heavy_order[i];
+                sm.desc = P.insts[slot];
+                sm.slice = P.slices ? P.slices[slot] : P.slice_iters;
+            }
             __syncthreads();
             dispatch<KINDS>(P, sm, tm);
         }
@@ -1172,7 +1179,11 @@ __global__ void __launch_bounds__(MAXT, 1) search_kernel(LaunchParams P) {
         __syncthreads();
         const uint32_t i = sm.inst;
         if (i >= P.n_insts) break;
-        if (threadIdx.x == 0) sm.desc = P.insts[P.order ? P.order[i] : i];
+        if (threadIdx.x == 0) {
+            const uint32_t slot = P.order ? P.order[i] : i;
+            sm.desc = P.insts[slot];
+            sm.slice = P.slices ? P.slices[slot] : P.slice_iters;
+        }
         __syncthreads();
         dispatch<KINDS>(P, sm, TeamRef{1, 0, nullptr, nullptr});
         __syncthreads();

@@ -87,6 +87,7 @@ struct Request {
     uint64_t prior_expansions = 0;
     uint32_t prior_iterations = 0;
     uint64_t w_off = 0, w_bytes = 0;  // grid weights placed in the weights pool at submission
+    uint64_t exp_seen = 0;            // expansions in the current partition after the last step
     std::vector<unsigned long long> path;  // goal first
 };
 
@@ -213,6 +214,7 @@ int admit(gastar_server* s, cudaStream_t st) {
         r.slot = slot;
         r.part_off = off;
         r.part_bytes = plan.bytes;
+        r.exp_seen = 0;
         r.state = ACTIVE;
         s->slot_req[slot] = id;
         char* base = reinterpret_cast<char*>(s->arena.p) + off;
@@ -308,6 +310,7 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     c->promote_log2 = 18;
     c->admit_bypass = 1;
     c->weights_pool = 1;
+    c->weighted_slices = 1;
 }
 
 gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
@@ -360,7 +363,7 @@ gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg
             s->heavy_teams = 0;
     }
     if (!s->arena.ensure(budget) || !s->descs.ensure(sizeof(InstDesc) * m) ||
-        !s->ctls.ensure(sizeof(InstCtl) * m) || !s->order.ensure(sizeof(uint32_t) * m) ||
+        !s->ctls.ensure(sizeof(InstCtl) * m) || !s->order.ensure(2 * sizeof(uint32_t) * m) ||
         !s->counters.ensure(64) ||
         !cuda_ok(cudaMallocHost(&s->h_ctl, sizeof(InstCtl) * m), "cudaMallocHost")) {
         gastar_serve_destroy(s);
@@ -471,10 +474,36 @@ int gastar_serve_step(gastar_server* s) {
     };
     std::stable_sort(light.begin(), light.end(), by_est);
     std::stable_sort(heavy.begin(), heavy.end(), by_est);
-    std::vector<uint32_t> order = light;
-    order.insert(order.end(), heavy.begin(), heavy.end());
-    const uint32_t n = (uint32_t)order.size();
-    if (!cuda_ok(cudaMemcpyAsync(s->order.p, order.data(), 4ull * n, cudaMemcpyHostToDevice, st),
+    // The order array (one-block requests, then heavy ones), then, at the end
+    // of a burst -- nothing but heavy requests left -- a slice length per
+    // slot: 1/2x to 4x the configured slice in proportion to each request's
+    // estimated work left (its one-block estimate less ~100 ns per expansion
+    // done), so that the largest grids do not all finish last, each on its
+    // own team while the other teams idle.
+    std::vector<uint32_t> order(light.size() + heavy.size() + s->max_active);
+    std::copy(light.begin(), light.end(), order.begin());
+    std::copy(heavy.begin(), heavy.end(), order.begin() + light.size());
+    const uint32_t n = (uint32_t)(light.size() + heavy.size());
+    bool weighted = false;
+    if (s->cfg.weighted_slices && light.empty() && s->waiting.empty() && heavy.size() > 1) {
+        std::vector<uint64_t> left(heavy.size());
+        for (size_t k = 0; k < heavy.size(); ++k) {
+            const Request& r = s->reqs[s->slot_req[heavy[k]]];
+            const uint64_t done = 100ull * (r.prior_expansions + r.exp_seen);
+            left[k] = std::max<uint64_t>(r.prob.est > done ? r.prob.est - done : 0, r.prob.est / 16 + 1);
+        }
+        std::vector<uint64_t> sorted(left);
+        std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 2, sorted.end());
+        const double med = (double)sorted[sorted.size() / 2];
+        const uint32_t base = s->cfg.slice_iters;
+        uint32_t* sl = order.data() + n;
+        for (uint32_t i = 0; i < s->max_active; ++i) sl[i] = base;
+        for (size_t k = 0; k < heavy.size(); ++k)
+            sl[heavy[k]] = (uint32_t)std::min(4.0 * base, std::max(0.5 * base, base * (double)left[k] / med));
+        weighted = true;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(s->order.p, order.data(), 4ull * (weighted ? n + s->max_active : n),
+                                 cudaMemcpyHostToDevice, st),
                  "cudaMemcpyAsync") ||
         !cuda_ok(cudaMemsetAsync(s->counters.p, 0, 32, st), "cudaMemsetAsync"))
         return GASTAR_CUDA_ERROR;
@@ -488,6 +517,7 @@ int gastar_serve_step(gastar_server* s) {
     P.next = reinterpret_cast<uint32_t*>(s->counters.p);
     P.team_ctas = 1;
     P.slice_iters = s->cfg.slice_iters;
+    P.slices = weighted ? reinterpret_cast<const uint32_t*>(s->order.p) + n : nullptr;
     P.barrier_timeout_ns = 2000000000ull;
     uint32_t blocks = std::min((uint32_t)light.size(), s->max_active);
     if (!heavy.empty()) {
@@ -530,6 +560,7 @@ int gastar_serve_step(gastar_server* s) {
     for (uint32_t slot : active) {
         const InstCtl& c = s->h_ctl[slot];
         Request& r = s->reqs[s->slot_req[slot]];
+        r.exp_seen = c.expansions;
         if (c.life != LIFE_DONE) {
             const uint32_t pl = s->cfg.promote_log2;
             if (pl && pl < 64 && r.prob.kind != KIND_GRID && r.prob.n >= 4 &&
