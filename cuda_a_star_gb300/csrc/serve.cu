@@ -474,18 +474,26 @@ int gastar_serve_step(gastar_server* s) {
     };
     std::stable_sort(light.begin(), light.end(), by_est);
     std::stable_sort(heavy.begin(), heavy.end(), by_est);
+    // Teams the launch can hold: one-block requests keep up to a quarter of
+    // the resident blocks (as many as there are of them), heavy requests get
+    // the rest in teams.
+    const uint32_t reserve = std::min<uint32_t>((uint32_t)light.size(), s->resident / 4);
+    const uint32_t team_cap =
+        std::min(std::max(1u, (s->resident - reserve) / std::max(1u, s->cfg.heavy_team)), s->heavy_teams);
     // The order array (one-block requests, then heavy ones), then, at the end
-    // of a burst -- nothing but heavy requests left -- a slice length per
-    // slot: 1/2x to 4x the configured slice in proportion to each request's
-    // estimated work left (its one-block estimate less ~100 ns per expansion
-    // done), so that the largest grids do not all finish last, each on its
-    // own team while the other teams idle.
+    // of a burst -- nothing but heavy requests left, more of them than teams,
+    // so that teams take turns -- a slice length per slot: 1/2x to 4x the
+    // configured slice in proportion to each request's estimated work left
+    // (its one-block estimate less ~100 ns per expansion done), so that the
+    // largest grids do not all finish last, each on its own team while the
+    // other teams idle.  With a team per request, equal slices keep every
+    // team busy until the launch ends.
     std::vector<uint32_t> order(light.size() + heavy.size() + s->max_active);
     std::copy(light.begin(), light.end(), order.begin());
     std::copy(heavy.begin(), heavy.end(), order.begin() + light.size());
     const uint32_t n = (uint32_t)(light.size() + heavy.size());
     bool weighted = false;
-    if (s->cfg.weighted_slices && light.empty() && s->waiting.empty() && heavy.size() > 1) {
+    if (s->cfg.weighted_slices && light.empty() && s->waiting.empty() && heavy.size() > team_cap) {
         std::vector<uint64_t> left(heavy.size());
         for (size_t k = 0; k < heavy.size(); ++k) {
             const Request& r = s->reqs[s->slot_req[heavy[k]]];
@@ -521,15 +529,11 @@ int gastar_serve_step(gastar_server* s) {
     P.barrier_timeout_ns = 2000000000ull;
     uint32_t blocks = std::min((uint32_t)light.size(), s->max_active);
     if (!heavy.empty()) {
-        // One-block requests keep up to a quarter of the resident blocks (as
-        // many as there are of them); heavy requests get the rest in teams.
         // Team blocks that run out of heavy requests take one-block requests,
         // and every block of the launch is resident (a cooperative launch),
         // so a team's blocks always run together.
         const uint32_t T = s->cfg.heavy_team;
-        const uint32_t reserve = std::min<uint32_t>((uint32_t)light.size(), s->resident / 4);
-        uint32_t teams = std::max(1u, (s->resident - reserve) / T);
-        teams = std::min({teams, s->heavy_teams, (uint32_t)heavy.size()});
+        const uint32_t teams = std::min(team_cap, (uint32_t)heavy.size());
         blocks = std::min(s->resident, teams * T + (uint32_t)light.size());
         P.heavy_order = reinterpret_cast<const uint32_t*>(s->order.p) + light.size();
         P.n_heavy = (uint32_t)heavy.size();

@@ -271,9 +271,10 @@ typedef struct gastar_serve_config {
                                   to a device pool (an eighth of the budget, beside it)
                                   at submission; 0, or a full pool = a host copy, sent
                                   at admission */
-    uint32_t weighted_slices;  /* 1 (default) = when only heavy requests are left (the end
-                                  of a burst), each gets 1/2x..4x slice_iters in
-                                  proportion to its estimated work left; 0 = equal */
+    uint32_t weighted_slices;  /* 1 (default) = when only heavy requests are left, more of
+                                  them than teams (the end of a burst), each gets
+                                  1/2x..4x slice_iters in proportion to its estimated
+                                  work left; 0 = equal */
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);
