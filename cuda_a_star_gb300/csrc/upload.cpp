@@ -124,10 +124,18 @@ void destroy_stager(HostStager* s) { delete s; }
 
 namespace {
 
+// Nothing may throw across the C ABI: a stager that cannot start its threads
+// or allocate reports failure, and the upload falls back to a copy.
 HostStager* stager(gastar_ctx* c) {
     if (c->stager) return c->stager;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    auto* s = new HostStager((int)std::min(8u, std::max(1u, hw / 2)) - 1);
+    HostStager* s = nullptr;
+    try {
+        s = new HostStager((int)std::min(8u, std::max(1u, hw / 2)) - 1);
+    } catch (...) {
+        set_error("grid upload: could not start the staging threads");
+        return nullptr;
+    }
     bool ok = cuda_ok(cudaMallocHost(reinterpret_cast<void**>(&s->pinned), HostStager::kChunk * HostStager::kSlots),
                       "cudaMallocHost");
     for (auto& e : s->ev) ok = ok && cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
@@ -159,10 +167,16 @@ int upload_grid_staged(gastar_ctx* c, uint8_t* d_dst, const uint8_t* h_src, uint
         const int parts = n >= (1u << 20) ? threads : 1;
         const size_t per = (n + parts - 1) / parts;
         const uint8_t* src = h_src + off;
-        hs->pool.run(parts, [&](int p) {
-            const size_t lo = (size_t)p * per, hi = std::min(n, lo + per);
-            part_min[p] = lo < hi ? copy_min_bytes(buf + lo, src + lo, hi - lo) : 255;
-        });
+        try {
+            hs->pool.run(parts, [&](int p) {
+                const size_t lo = (size_t)p * per, hi = std::min(n, lo + per);
+                part_min[p] = lo < hi ? copy_min_bytes(buf + lo, src + lo, hi - lo) : 255;
+            });
+        } catch (...) {  // std::function or locking failed: nothing was sent from this chunk
+            if (!cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return GASTAR_CUDA_ERROR;
+            set_error("grid upload: staging failed");
+            return GASTAR_CUDA_ERROR;
+        }
         for (int p = 0; p < parts; ++p) m = std::min(m, part_min[p]);
         if (!cuda_ok(cudaMemcpyAsync(d_dst + off, buf, n, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync") ||
             !cuda_ok(cudaEventRecord(hs->ev[slot], st), "cudaEventRecord"))
