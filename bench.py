@@ -872,7 +872,8 @@ def run_profile_case(kind: str) -> None:
     """Small copies of the workloads for ncu captures (a few GB on the device).
     plain: 4 of the 64 P15 instances, 2^24-slot table, one launch each.
     batched: 32 P15 (walk 20-80) + 32 grids (side 256-512), a run and a re-run.
-    grid: the 4096^2 grid solved twice (upload kernel, search, path rebuild)."""
+    grid: the 4096^2 grid solved twice (upload kernel, search, path rebuild).
+    served: two 4096^2 grids on eight-block teams in a server (2 GiB budget)."""
     import cuda_a_star_gb300 as g
     from cuda_a_star_gb300 import build as engine_build
     engine_build.build()
@@ -889,6 +890,19 @@ def run_profile_case(kind: str) -> None:
                                   "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
                                   "iterations": r.iterations, "kernel_ms": r.kernel_ms,
                                   "algorithmic_bytes": alg(r)}))
+            return
+        if kind == "served":
+            srv = eng.server(budget_bytes=2 << 30)
+            reqs = [g.gen_grid(4096, 4096, 0x5E00 + i, 0.2) for i in range(2)]
+            ids = [srv.submit_grid(w, (0, 0), (4095, 4095)) for w in reqs]
+            out = srv.drain(ids)
+            for i in ids:
+                r = out[i]
+                print(json.dumps({"status": r.status_name, "cost": r.cost, "expansions": r.expansions,
+                                  "generated": r.generated, "pushes": r.pushes, "stale": r.stale,
+                                  "iterations": r.iterations, "algorithmic_bytes": alg(r)}))
+            print(json.dumps({"search_kernel_ms": srv.stats()["kernel_ms"]}))
+            srv.close()
             return
         if kind == "grid":
             wts = g.gen_grid(4096, 4096, 0x4096, 0.2)
@@ -932,7 +946,7 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the reference's own CUDA GA* beside the engine on small grids")
     ap.add_argument("--reference-gpu-case", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--profile-case", nargs="?", const="plain", choices=["plain", "batched", "grid"],
+    ap.add_argument("--profile-case", nargs="?", const="plain", choices=["plain", "batched", "grid", "served"],
                     help="small single pass for ncu captures (no bench JSON line)")
     ap.add_argument("--random-sweep", action="store_true",
                     help="print the random-access rate over buffer size, depth in flight and "
