@@ -73,7 +73,7 @@ class ServeConfig(C.Structure):
         ("heavy_team", C.c_uint32), ("heavy_teams", C.c_uint32), ("heavy_cells", C.c_uint64),
         ("open_list", C.c_uint32), ("promote_log2", C.c_uint32),
         ("admit_bypass", C.c_uint32), ("weights_pool", C.c_uint32),
-        ("weighted_slices", C.c_uint32),
+        ("weighted_slices", C.c_uint32), ("heavy_set", C.c_uint32),
     ]
 
 

@@ -311,6 +311,7 @@ void gastar_serve_config_default(gastar_serve_config* c) {
     c->admit_bypass = 1;
     c->weights_pool = 1;
     c->weighted_slices = 1;
+    c->heavy_set = 4;
 }
 
 gastar_server* gastar_serve_create(gastar_ctx* c, const gastar_serve_config* cfg) {
@@ -536,7 +537,14 @@ int gastar_serve_step(gastar_server* s) {
         const uint32_t teams = std::min(team_cap, (uint32_t)heavy.size());
         blocks = std::min(s->resident, teams * T + (uint32_t)light.size());
         P.heavy_order = reinterpret_cast<const uint32_t*>(s->order.p) + light.size();
+        // At most heavy_set x teams heavy requests, the largest first, take
+        // turns in a launch: fewer grids per launch keep their frontiers in
+        // L2 between slices (burst capacity 267 against 252 req/s with all;
+        // 2x the teams: 226, 3x: 251, 6x: 257); the teams still share them
+        // dynamically, and the rest run as the largest finish.
         P.n_heavy = (uint32_t)heavy.size();
+        if (s->cfg.heavy_set)
+            P.n_heavy = (uint32_t)std::min<uint64_t>(heavy.size(), (uint64_t)s->cfg.heavy_set * teams);
         P.heavy_team = s->cfg.heavy_team;
         P.heavy_teams = teams;
         P.heavy_next = reinterpret_cast<uint32_t*>(s->counters.p) + 4;

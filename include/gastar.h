@@ -275,6 +275,10 @@ typedef struct gastar_serve_config {
                                   them than teams (the end of a burst), each gets
                                   1/2x..4x slice_iters in proportion to its estimated
                                   work left; 0 = equal */
+    uint32_t heavy_set;        /* at most heavy_set x teams heavy requests, the largest
+                                  first, take turns on the teams in a launch (default 4:
+                                  fewer grids per launch keep their frontiers in L2);
+                                  0 = all active ones */
 } gastar_serve_config;
 
 void gastar_serve_config_default(gastar_serve_config *cfg);
